@@ -1,0 +1,400 @@
+#!/usr/bin/env python3
+"""bench.py -- exact polynomial-matrix product (and pmbasis) on one GB300.
+
+Headline workload: nmod_poly_mat_mul of two 64x64 polynomial matrices, every
+entry of length 4096 (degree < 4096), p = 998244353, coefficients uniform in
+[0, p) from a seed (uint64 storage): forward NTT of length 8192, 8192 pointwise
+64x64x64 products mod p, inverse NTT.  One "step" = one full product.
+`value` is the time of one product with the split-limb INT8 tensor-core form,
+inputs resident in HBM (267 MB of inputs, larger than L2, so no flush is
+needed); the same product with the CUDA-core form is reported beside it, and
+pmbasis of a 64x32 matrix at order 8192 (zero shift) for both forms.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pml|reference]
+
+With N > 1 (torchrun, one rank per GPU) every rank runs an independent
+replica (the product does not shard across GPUs here): barrier + max over
+ranks, rank 0 prints.  --impl reference times the CPU restatement of the
+reference algorithm (the reference itself needs FLINT, which is not
+installed) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+P = 998244353
+R = K = C = 64
+LEN = 4096
+PM_M, PM_N, PM_ORDER = 64, 32, 8192
+WORKLOAD = "nmod_poly_mat_mul 64x64 . 64x64, len 4096 (deg < 4096), p = 998244353, uniform coefficients"
+METRIC = "exact poly_mat_mul & pmbasis time: INT8 split-limb TC vs CUDA-core form, 1 GB300"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["pml", "reference"], default="pml")
+    ap.add_argument("--no-pmbasis", action="store_true", help="skip the pmbasis measurement")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_inputs(seed: int):
+    """Seeded synthetic inputs: uniform in [0, p) (numpy PCG64)."""
+    rng = np.random.default_rng(seed)
+    A = rng.integers(0, P, size=(R, K, LEN), dtype=np.uint64)
+    B = rng.integers(0, P, size=(K, C, LEN), dtype=np.uint64)
+    return A, B
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.device)], stdout=self.fh, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (oracle port: the reference's algorithm restated in C)
+# ---------------------------------------------------------------------------
+
+def cpu_product_ms(nthreads: int, reps: int, warm: int):
+    import oracle
+    A, B = make_inputs(1)
+    t = []
+    for i in range(warm + reps):
+        t0 = time.perf_counter()
+        oracle.poly_mat_mul_ntt(A, B, P, nthreads=nthreads)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i >= warm:
+            t.append(dt)
+    return statistics.median(t), t
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    nthreads = os.cpu_count() or 1
+    med, ts = cpu_product_ms(nthreads, max(args.steps, 1), max(args.warmup, 0))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": med, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": med, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded uniform [0,p))",
+        "config": {"workload": WORKLOAD, "implementation": "CPU evaluation/interpolation product (NTT at "
+                   "2^13-th roots of unity, one 64x64 matrix product mod p per point), C restatement of "
+                   "flint-extras mul_geometric.c; FLINT/PML themselves are not installed",
+                   "threads": nthreads},
+        "cpu_baseline": {"value": med, "unit": "ms", "cores": nthreads, "kind": "port",
+                         "sample": f"full product per step, {nthreads} OpenMP threads"},
+        "e2e": {"value": med, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU leg
+# ---------------------------------------------------------------------------
+
+def algorithmic_bytes(kernel: str):
+    """Algorithmic HBM bytes (or int8 ops) per launch of each kernel at the headline workload."""
+    N = 8192
+    ent_in = R * K            # = K * C
+    if kernel == "ntt_fwd":
+        return ("hbm", ent_in * (LEN * 8 + N * 4))          # read uint64 coefficients, write uint32 evaluations
+    if kernel == "ntt_inv":
+        return ("hbm", R * C * (N * 4 + (2 * LEN - 1) * 8))  # read evaluations, write uint64 coefficients
+    if kernel == "pointwise_int8_tc":
+        return ("tensor", 2 * 16 * N * R * K * C)           # 16 limb products per MAC, 2 ops per MAC
+    if kernel == "pointwise_cuda_core":
+        return ("hbm", 3 * N * R * C * 4)
+    return ("hbm", None)
+
+
+def run_pml(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import pml_gb300
+    from pml_gb300 import _lib
+
+    ctx = pml_gb300.Context(local)
+    st = torch.cuda.current_stream(dev)
+
+    A, B = make_inputs(1 + rank)
+    dA = torch.from_numpy(A.view(np.int64)).to(dev)
+    dB = torch.from_numpy(B.view(np.int64)).to(dev)
+    dC = torch.empty((R, C, 2 * LEN - 1), dtype=torch.int64, device=dev)
+
+    def step():
+        ctx.check(ctx.lib.pmlg_poly_mat_mul(ctx.handle, dC.data_ptr(), dA.data_ptr(), dB.data_ptr(),
+                                            R, K, C, LEN, LEN, P, st.cuda_stream))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def timed(form: int, steps: int, warmup: int, clocks=False):
+        ctx.set_form(form)
+        for _ in range(warmup):
+            step()
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if clocks else None
+        if sampler:
+            sampler.__enter__()
+        l0 = ctx.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(steps):
+            step()
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier()
+        torch.cuda.synchronize()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        ms = e0.elapsed_time(e1) / steps
+        return max_over_ranks(ms), ctx.launches - l0, (sampler.summary() if sampler else None)
+
+    # correctness spot-check of this exact workload before timing: both forms equal
+    ctx.set_form(pml_gb300.FORM_CUDA_CORE)
+    step()
+    ref = dC.clone()
+    ctx.set_form(pml_gb300.FORM_INT8_TC)
+    step()
+    torch.cuda.synchronize()
+    forms_agree = bool(torch.equal(ref, dC))
+    del ref
+
+    ms_i8, launches, clocks = timed(pml_gb300.FORM_INT8_TC, args.steps, args.warmup, clocks=True)
+    ms_cc, _, _ = timed(pml_gb300.FORM_CUDA_CORE, args.steps, args.warmup)
+
+    # per-kernel device times (separate pass, events on the launch stream)
+    def kernel_profile(form: int, steps: int):
+        ctx.set_form(form)
+        step()
+        torch.cuda.synchronize()
+        ctx.set_profiling(True)
+        for _ in range(steps):
+            step()
+        torch.cuda.synchronize()
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        return prof
+
+    prof_i8 = kernel_profile(pml_gb300.FORM_INT8_TC, args.steps)
+    prof_cc = kernel_profile(pml_gb300.FORM_CUDA_CORE, args.steps)
+
+    def summarize(prof):
+        tot = sum(v[0] for v in prof.values()) or 1.0
+        return {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / tot} for k, v in prof.items()}
+
+    kern_i8 = summarize(prof_i8)
+    dom = max(prof_i8, key=lambda k: prof_i8[k][0])
+    bound, work = algorithmic_bytes(dom)
+    avg_s = prof_i8[dom][0] / prof_i8[dom][1] / 1e3
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    roofline = None
+    if work is not None:
+        if bound == "hbm":
+            peak = peaks.get("hbm_gbs", 6800.0)
+            ach = work / avg_s / 1e9
+            roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
+                        "frac": ach / peak, "traffic": None,
+                        "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                        "algorithmic_bytes_per_launch": work}
+        else:
+            peak = peaks.get("bf16_tflops", 1900.0)
+            ach = work / avg_s / 1e12
+            roofline = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                        "frac": ach / peak, "traffic": None,
+                        "peak_source": "measured dense bf16 (no measured INT8 peak exists for this pool)",
+                        "algorithmic_ops_per_launch": work}
+
+    # end to end through the host-buffer entry point, pinned host memory
+    hA = torch.from_numpy(A.view(np.int64)).pin_memory()
+    hB = torch.from_numpy(B.view(np.int64)).pin_memory()
+    hC = torch.empty((R, C, 2 * LEN - 1), dtype=torch.int64).pin_memory()
+    ctx.set_form(pml_gb300.FORM_INT8_TC)
+
+    def e2e_step():
+        ctx.check(ctx.lib.pmlg_poly_mat_mul_host(ctx.handle, hC.data_ptr(), hA.data_ptr(), hB.data_ptr(),
+                                                 R, K, C, LEN, LEN, P, st.cuda_stream))
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    e2e_ok = bool(torch.equal(hC, dC.cpu()))
+    h2d = 2 * R * K * LEN * 8
+    d2h = R * C * (2 * LEN - 1) * 8
+
+    # pmbasis 64x32, order 8192, both forms (one warm-up call, one timed call each)
+    pm = None
+    if not args.no_pmbasis:
+        rng = np.random.default_rng(7 + rank)
+        F = rng.integers(0, P, size=(PM_M, PM_N, PM_ORDER), dtype=np.uint64)
+        dF = torch.from_numpy(F.view(np.int64)).to(dev)
+        pm = {}
+        outs = {}
+        for name, form in (("int8_tc", pml_gb300.FORM_INT8_TC), ("cuda_core", pml_gb300.FORM_CUDA_CORE)):
+            ctx.set_form(form)
+            pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            ab, sh = pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
+            torch.cuda.synchronize()
+            pm[name + "_ms"] = max_over_ranks((time.perf_counter() - t0) * 1e3)
+            outs[name] = (ab, sh)
+        ctx.set_profiling(True)
+        ctx.set_form(pml_gb300.FORM_INT8_TC)
+        pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        pm["kernels_int8_tc"] = summarize(prof)
+        pm["forms_agree"] = bool(torch.equal(outs["int8_tc"][0], outs["cuda_core"][0])
+                                 and list(outs["int8_tc"][1]) == list(outs["cuda_core"][1]))
+        pm["speedup_int8_vs_cuda_core"] = pm["cuda_core_ms"] / pm["int8_tc_ms"]
+        pm["config"] = "pmbasis 64x32, order 8192, zero shift, p = 998244353, uniform coefficients"
+        pm["timing"] = "wall clock around one call (it synchronises internally), after one warm-up call"
+
+    # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        med, ts = cpu_product_ms(1, 1, 0)
+        cpu = {"value": med, "unit": "ms", "cores": 1, "kind": "port",
+               "sample": "one full 64x64 len-4096 product, CPU evaluation/interpolation port (C, 1 thread)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms_i8, "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_i8, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded uniform [0,p), numpy PCG64)",
+            "config": {"workload": WORKLOAD, "form": "int8_tc (mma.sync u8 limbs, s32 accumulate)",
+                       "parallelism": f"replicas x{world}", "l2": "inputs 268 MB > 129 MB L2, no flush",
+                       "transform": "N = 8192, 2 x 4096 forward + 4096 inverse NTTs"},
+            "cuda_core_ms": ms_cc, "speedup_int8_vs_cuda_core": ms_cc / ms_i8, "forms_agree": forms_agree,
+            "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "path": "pmlg_poly_mat_mul_host, pinned host buffers", "matches_device": e2e_ok},
+            "gpu_launches": launches,
+            "roofline": roofline,
+            "kernels": {"int8_tc": kern_i8, "cuda_core": summarize(prof_cc)},
+            "clocks": clocks,
+            "pmbasis": pm,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_pml(args)
+
+
+if __name__ == "__main__":
+    main()

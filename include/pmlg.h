@@ -1,0 +1,214 @@
+/*
+ * pmlg.h -- C ABI of pml-gb300: the evaluation/interpolation hot path of PML
+ * (polynomial matrices over Z/pZ) on one GB300 (sm_103a).
+ *
+ * Every entry point is a plain C function over plain pointers and sizes.
+ * Functions named *_host take host buffers and do the host<->device copies
+ * themselves; all others take DEVICE pointers and run stream-ordered on the
+ * given cudaStream_t (passed as void*, NULL = legacy default stream).
+ *
+ * Layouts (dense, zero padded, the coefficient arrays of FLINT's nmod_poly
+ * entries laid side by side):
+ *   matrix       : row-major, M[i*c + j]
+ *   poly matrix  : entry-major, P[(i*c + j)*len + d] = coefficient d of entry (i,j)
+ * Coefficients are uint64_t in [0, p) (FLINT ulong), 2 <= p < 2^64, unless a
+ * function says uint32_t.  Inputs must be reduced mod p, as FLINT requires.
+ *
+ * Return value: PMLG_OK (0) or a PMLG_E* status; nothing aborts.  After an
+ * error, pmlg_ctx_last_error() describes it.
+ */
+#ifndef PMLG_H
+#define PMLG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define PMLG_API __attribute__((visibility("default")))
+#else
+#define PMLG_API
+#endif
+
+typedef struct pmlg_ctx pmlg_ctx;
+
+enum pmlg_status_code
+{
+    PMLG_OK = 0,
+    PMLG_EINVAL = 1,     /* bad argument (negative size, null pointer, ...) */
+    PMLG_EBADMOD = 2,    /* modulus not supported by this entry point */
+    PMLG_ENOROOT = 3,    /* no root of unity of the needed order */
+    PMLG_ELEN = 4,       /* length beyond the supported transform size */
+    PMLG_EALIAS = 5,     /* output overlaps an input where that is not allowed */
+    PMLG_ETIMEOUT = 6,   /* a bounded device wait gave up */
+    PMLG_ECUDA = 7,      /* CUDA runtime error */
+    PMLG_ENOMEM = 8,     /* device or host allocation failed */
+    PMLG_EUNSUP = 9      /* shape outside what this build supports */
+};
+
+/* Which kernel form computes the pointwise matrix products. */
+enum pmlg_form
+{
+    PMLG_FORM_AUTO = 0,       /* library choice (fastest measured) */
+    PMLG_FORM_CUDA_CORE = 1,  /* uint64 multiply-accumulate with delayed reduction */
+    PMLG_FORM_INT8_TC = 2     /* 8-bit limbs on the INT8 tensor cores (mma.sync, s32 accumulate) */
+};
+
+/* ---------------------------------------------------------------------- */
+/* context                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Creates a context on `device`: holds the NTT tables per (prime, length), the
+ * device scratch and pinned staging buffers.  One context per host thread. */
+PMLG_API int pmlg_ctx_create(pmlg_ctx **ctx, int device);
+PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx);
+PMLG_API int pmlg_ctx_set_form(pmlg_ctx *ctx, int form);
+/* pmbasis leaf order (mbasis below it); 0 restores the tuned default */
+PMLG_API int pmlg_ctx_set_leaf_order(pmlg_ctx *ctx, int64_t order);
+/* number of kernels this context has launched so far */
+PMLG_API unsigned long long pmlg_ctx_launch_count(const pmlg_ctx *ctx);
+PMLG_API const char *pmlg_ctx_last_error(const pmlg_ctx *ctx);
+/* Kernel timing (tracing): when on, every kernel launched through the context
+ * is bracketed by CUDA events recorded on its own stream.  set_profiling also
+ * clears the records.  profile_read synchronises on the recorded events and
+ * returns, per kernel name, the summed device time in ms and the launch count
+ * (names '\n'-separated in `names`).  Plays the role of the reference's
+ * MBASIS_PROFILE timers (nmod_mat_poly_mbasis.c:9-57). */
+PMLG_API int pmlg_ctx_set_profiling(pmlg_ctx *ctx, int on);
+PMLG_API int pmlg_ctx_profile_read(pmlg_ctx *ctx, char *names, size_t names_len, double *ms,
+                                   unsigned long long *counts, int max_kernels, int *n_out);
+PMLG_API const char *pmlg_strerror(int status);
+
+/* ---------------------------------------------------------------------- */
+/* L2: batched matrix products mod p at the evaluation points              */
+/* ---------------------------------------------------------------------- */
+
+/* C[b] = A[b] * B[b] mod p for b < nbatch; A[b] r x k, B[b] k x c, C[b] r x c,
+ * row-major, stored contiguously batch after batch, uint32 storage.
+ * Requires p < 2^30 (any p, prime or not).  Replaces the per-point FLINT
+ * nmod_mat_mul loop of flint-extras/src/nmod_poly_mat_extra/mul_geometric.c:95-96
+ * (and mulmid.c:105-106, 200-201).  Uses the context's form. */
+PMLG_API int pmlg_nmod_mat_mul_batch_u32(pmlg_ctx *ctx, uint32_t *C, const uint32_t *A,
+                                         const uint32_t *B, int64_t nbatch, int64_t r,
+                                         int64_t k, int64_t c, uint64_t p, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* L3: polynomial matrix products                                          */
+/* ---------------------------------------------------------------------- */
+
+/* C = A * B.  A: r x k of capacity len1; B: k x c of capacity len2;
+ * C: r x c of capacity len1 + len2 - 1 (fully written).
+ * Replaces nmod_poly_mat_multiply (flint-extras/src/nmod_poly_mat_extra/mul.c:19-97)
+ * and nmod_poly_mat_mul_geometric (mul_geometric.c:121-157).
+ * C may not overlap A or B (PMLG_EALIAS); callers that alias use a temporary,
+ * as mul.c:42-50 does. */
+PMLG_API int pmlg_poly_mat_mul(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B,
+                               int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                               uint64_t p, void *stream);
+
+/* res = (A * B mod x^nhi) div x^nlo, res of capacity nhi - nlo (fully written,
+ * zero beyond the clamped length).  *out_len (host, may be NULL) receives the
+ * clamped length max(0, min(nhi, L1+L2-1) - nlo), L1/L2 the actual max lengths
+ * of A/B, as nmod_poly_mat_mulmid (mulmid.c:499-541) computes it; computing it
+ * needs a device->host read, so pass NULL to keep the call asynchronous.
+ * Replaces nmod_poly_mat_mulmid / _nmod_poly_mat_mulmid (mulmid.c:470-541). */
+PMLG_API int pmlg_poly_mat_mulmid(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A,
+                                  const uint64_t *B, int64_t r, int64_t k, int64_t c,
+                                  int64_t len1, int64_t len2, int64_t nlo, int64_t nhi,
+                                  uint64_t p, int64_t *out_len, void *stream);
+
+/* Host-buffer forms of the two products: copies inputs to the device, computes,
+ * copies the result back, synchronises `stream`. */
+PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A,
+                                    const uint64_t *B, int64_t r, int64_t k, int64_t c,
+                                    int64_t len1, int64_t len2, uint64_t p, void *stream);
+PMLG_API int pmlg_poly_mat_mulmid_host(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A,
+                                       const uint64_t *B, int64_t r, int64_t k, int64_t c,
+                                       int64_t len1, int64_t len2, int64_t nlo, int64_t nhi,
+                                       uint64_t p, int64_t *out_len, void *stream);
+
+/* A batch of independent products C_i = A_i * B_i with their own shapes,
+ * lengths and moduli, computed together (one launch sequence for the whole
+ * batch).  Device pointers.  Replaces a loop of nmod_poly_mat_multiply calls. */
+typedef struct pmlg_polymat_job
+{
+    int64_t r, k, c, len1, len2;
+    uint64_t p;
+    const uint64_t *A;
+    const uint64_t *B;
+    uint64_t *C;            /* capacity len1 + len2 - 1 */
+} pmlg_polymat_job;
+
+PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs, int64_t njobs,
+                                     void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* L4: approximant bases                                                   */
+/* ---------------------------------------------------------------------- */
+
+/* Approximant basis of F (m x n, capacity flen, device) at `order` for the
+ * shift `shift` (host, m entries; in: input shift, out: shifted row degree).
+ * appbas: device, m x m of capacity appbas_cap >= order + 1 (fully written).
+ * *appbas_len (host, may be NULL) receives the max length of appbas.
+ * p must be a prime < 2^30.  The stream is synchronised before return.
+ * pmlg_pmbasis replaces nmod_poly_mat_pmbasis
+ * (flint-extras/src/nmod_poly_mat_extra/approximant_basis.c:33-69);
+ * pmlg_mbasis replaces nmod_poly_mat_mbasis (approximant_basis.c:18-31,
+ * nmod_mat_poly_extra/nmod_mat_poly_mbasis.c:116-378). */
+PMLG_API int pmlg_pmbasis(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
+                          const uint64_t *F, int64_t m, int64_t n, int64_t flen, int64_t order,
+                          uint64_t p, int64_t *appbas_len, void *stream);
+PMLG_API int pmlg_mbasis(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
+                         const uint64_t *F, int64_t m, int64_t n, int64_t flen, int64_t order,
+                         uint64_t p, int64_t *appbas_len, void *stream);
+/* Host-buffer form of pmlg_pmbasis. */
+PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
+                               const uint64_t *F, int64_t m, int64_t n, int64_t flen,
+                               int64_t order, uint64_t p, int64_t *appbas_len, void *stream);
+
+/* ---------------------------------------------------------------------- */
+/* L1: modular dot products and multimodular reduction / CRT               */
+/* ---------------------------------------------------------------------- */
+
+/* res[0] (device) = sum_{i<len} v1[i]*v2[i] mod p; entries are arbitrary 64-bit
+ * words (not assumed reduced), any 2 <= p < 2^64.
+ * Replaces nmod_vec_dot_product_unbalanced
+ * (flint-extras/src/nmod_vec_extra/nmod_vec_dot_product.c:136-147) with full
+ * 64-bit inputs (the max_bits arguments only bound the accumulator there). */
+PMLG_API int pmlg_nmod_vec_dot(pmlg_ctx *ctx, uint64_t *res, const uint64_t *v1,
+                               const uint64_t *v2, int64_t len, uint64_t p, void *stream);
+/* 32-bit storage, p <= 2^32: replaces _nmod32_vec_dot_split
+ * (flint-extras/src/nmod32_vec/dot_split.c:18-47) without its length limit. */
+PMLG_API int pmlg_nmod32_vec_dot(pmlg_ctx *ctx, uint32_t *res, const uint32_t *v1,
+                                 const uint32_t *v2, int64_t len, uint64_t p, void *stream);
+/* mv[i] = sum_{j<len} mat[i*stride + j] * vec[j] mod p, i < nrows, 32-bit storage:
+ * replaces _nmod32_vec_mdot_split (flint-extras/src/nmod32_vec/mdot_split.c:17-26). */
+PMLG_API int pmlg_nmod32_vec_mdot(pmlg_ctx *ctx, uint32_t *mv, const uint32_t *mat,
+                                  const uint32_t *vec, int64_t nrows, int64_t len,
+                                  int64_t stride, uint64_t p, void *stream);
+/* uv[j] = sum_{i<len} u[i] * v[i*k + j] mod p, j < k (vector-matrix product),
+ * 64-bit entries: replaces nmod_vec_dot_product_multi
+ * (flint-extras/src/nmod_vec_extra/nmod_vec_dot_product_multi.c:2054), with the
+ * rows of v stored contiguously instead of as an array of row pointers. */
+PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t *u,
+                                     const uint64_t *v, int64_t len, int64_t k, uint64_t p,
+                                     void *stream);
+
+/* residues[j*nb + i] = input[i] mod primes[j], j < nprimes <= 6, primes < 2^63:
+ * replaces nmod_multimod_CRT_reduce (flint-extras/src/nmod_extra/nmod_multimod_CRT_reduce.c:22). */
+PMLG_API int pmlg_multimod_reduce(pmlg_ctx *ctx, uint64_t *residues, const uint64_t *input,
+                                  int64_t nb, const uint64_t *primes, int nprimes, void *stream);
+/* out[i] = CRT(residues[j*nb + i], j < nprimes) mod p, the CRT value taken in
+ * [0, prod primes); primes pairwise coprime, < 2^63:
+ * replaces nmod_multimod_CRT_CRT (flint-extras/src/nmod_extra/nmod_multimod_CRT_CRT.c:509). */
+PMLG_API int pmlg_multimod_crt(pmlg_ctx *ctx, uint64_t *out, const uint64_t *residues,
+                               int64_t nb, const uint64_t *primes, int nprimes, uint64_t p,
+                               void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PMLG_H */

@@ -1,0 +1,331 @@
+"""pml_gb300 -- GB300 (sm_103a) implementation of PML's evaluation/interpolation
+hot path for polynomial matrices over Z/pZ.
+
+The compute is the CUDA library libpmlg.so (C ABI, include/pmlg.h).  This
+module is its host-side mirror of the reference interface: the functions keep
+the flint-extras names (nmod_poly_mat_multiply, nmod_poly_mat_mulmid,
+nmod_poly_mat_pmbasis, nmod_poly_mat_mbasis, nmod_vec_dot_product, ...) and
+their argument meaning, over dense arrays instead of FLINT structs:
+
+* a polynomial matrix is an array of shape (rows, cols, len), entry-major,
+  coefficients in [0, p) stored as uint64 (torch.int64 holding the same bits
+  on the GPU, numpy.uint64 on the host);
+* device tensors are processed on the current torch CUDA stream; numpy arrays
+  go through the *_host entry points (copies included).
+
+There is no CPU fallback: every function calls libpmlg.so and raises
+PmlgError on a non-zero status.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_INT8_TC, PmlgError, PolymatJob, check
+
+__all__ = [
+    "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC",
+    "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
+    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_vec_dot_product", "nmod32_vec_dot_product",
+    "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
+]
+
+
+class Context:
+    """A pmlg_ctx: NTT tables, scratch memory and the pointwise-product form."""
+
+    def __init__(self, device: int = 0, form: int = FORM_AUTO, leaf_order: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        check(self.lib.pmlg_ctx_create(C.byref(h), device))
+        self.handle = h
+        self.device = device
+        self.set_form(form)
+        if leaf_order:
+            self.set_leaf_order(leaf_order)
+
+    def set_form(self, form: int) -> None:
+        check(self.lib.pmlg_ctx_set_form(self.handle, form), self.handle)
+        self.form = form
+
+    def set_leaf_order(self, order: int) -> None:
+        check(self.lib.pmlg_ctx_set_leaf_order(self.handle, order), self.handle)
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.pmlg_ctx_launch_count(self.handle))
+
+    def check(self, status: int) -> None:
+        check(status, self.handle)
+
+    def set_profiling(self, on: bool) -> None:
+        """Bracket every kernel launch with CUDA events on its stream (and clear
+        earlier records)."""
+        check(self.lib.pmlg_ctx_set_profiling(self.handle, 1 if on else 0), self.handle)
+
+    def profile(self) -> dict:
+        """{kernel name: (total device ms, launches)} since set_profiling(True)."""
+        nmax = 64
+        names = C.create_string_buffer(8192)
+        ms = (C.c_double * nmax)()
+        cnt = (C.c_ulonglong * nmax)()
+        n = C.c_int(0)
+        check(self.lib.pmlg_ctx_profile_read(self.handle, names, 8192, ms, cnt, nmax, C.byref(n)), self.handle)
+        keys = names.value.decode().split("\n")
+        return {keys[i]: (ms[i], int(cnt[i])) for i in range(n.value)}
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.pmlg_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default: dict[int, Context] = {}
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default:
+        _default[device] = Context(device)
+    return _default[device]
+
+
+def _stream_ptr(t) -> int:
+    import torch
+    return torch.cuda.current_stream(t.device).cuda_stream
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _ptr(t) -> int:
+    return t.data_ptr() if _is_torch(t) else t.ctypes.data
+
+
+def _ctx(ctx: Optional[Context], t=None) -> Context:
+    if ctx is not None:
+        return ctx
+    dev = t.device.index if (t is not None and _is_torch(t) and t.device.index is not None) else 0
+    return default_context(dev)
+
+
+def _require_cuda(*ts):
+    for t in ts:
+        if not (_is_torch(t) and t.is_cuda and t.is_contiguous()):
+            raise TypeError("expected contiguous CUDA tensors")
+
+
+# ---------------------------------------------------------------------------
+# L2: batched matrix products mod p
+# ---------------------------------------------------------------------------
+
+def nmod_mat_mul_batch(A, B, p: int, ctx: Optional[Context] = None):
+    """C[b] = A[b] @ B[b] mod p, uint32 storage (torch.int32 CUDA tensors of shape
+    (nb, r, k) and (nb, k, c)); p < 2^30.  Per-point nmod_mat_mul of
+    mul_geometric.c:95-96."""
+    import torch
+    _require_cuda(A, B)
+    nb, r, k = A.shape
+    nb2, k2, c = B.shape
+    assert nb == nb2 and k == k2
+    ctx = _ctx(ctx, A)
+    out = torch.empty((nb, r, c), dtype=A.dtype, device=A.device)
+    ctx.check(ctx.lib.pmlg_nmod_mat_mul_batch_u32(ctx.handle, _ptr(out), _ptr(A), _ptr(B), nb, r, k, c, p,
+                                                  _stream_ptr(A)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# L3: products
+# ---------------------------------------------------------------------------
+
+def nmod_poly_mat_multiply(A, B, p: int, ctx: Optional[Context] = None, out=None):
+    """res = A * B (nmod_poly_mat_multiply, mul.c:19).  A: (r, k, len1), B: (k, c, len2);
+    returns (r, c, len1 + len2 - 1).  CUDA tensors run on the current stream;
+    numpy arrays use the host-buffer entry point."""
+    r, k, l1 = A.shape
+    k2, c, l2 = B.shape
+    if k != k2:
+        raise ValueError("inner dimensions differ")
+    clen = l1 + l2 - 1 if (l1 > 0 and l2 > 0) else 0
+    ctx = _ctx(ctx, A)
+    if _is_torch(A):
+        import torch
+        _require_cuda(A, B)
+        if out is None:
+            out = torch.empty((r, c, clen), dtype=torch.int64, device=A.device)
+        ctx.check(ctx.lib.pmlg_poly_mat_mul(ctx.handle, _ptr(out), _ptr(A), _ptr(B), r, k, c, l1, l2, p,
+                                            _stream_ptr(A)))
+        return out
+    A = np.ascontiguousarray(A, dtype=np.uint64)
+    B = np.ascontiguousarray(B, dtype=np.uint64)
+    if out is None:
+        out = np.empty((r, c, clen), dtype=np.uint64)
+    ctx.check(ctx.lib.pmlg_poly_mat_mul_host(ctx.handle, _ptr(out), _ptr(A), _ptr(B), r, k, c, l1, l2, p, None))
+    return out
+
+
+def nmod_poly_mat_mulmid(A, B, nlo: int, nhi: int, p: int, ctx: Optional[Context] = None,
+                         want_length: bool = False):
+    """res = (A * B mod x^nhi) div x^nlo (nmod_poly_mat_mulmid, mulmid.c:499).
+    Returns the (r, c, nhi - nlo) array, and with want_length the clamped length."""
+    r, k, l1 = A.shape
+    _, c, l2 = B.shape
+    cap = max(nhi - nlo, 0)
+    ctx = _ctx(ctx, A)
+    n = C.c_int64(0)
+    nptr = C.byref(n) if want_length else None
+    if _is_torch(A):
+        import torch
+        _require_cuda(A, B)
+        out = torch.empty((r, c, cap), dtype=torch.int64, device=A.device)
+        ctx.check(ctx.lib.pmlg_poly_mat_mulmid(ctx.handle, _ptr(out), _ptr(A), _ptr(B), r, k, c, l1, l2, nlo, nhi,
+                                               p, nptr, _stream_ptr(A)))
+    else:
+        A = np.ascontiguousarray(A, dtype=np.uint64)
+        B = np.ascontiguousarray(B, dtype=np.uint64)
+        out = np.empty((r, c, cap), dtype=np.uint64)
+        ctx.check(ctx.lib.pmlg_poly_mat_mulmid_host(ctx.handle, _ptr(out), _ptr(A), _ptr(B), r, k, c, l1, l2, nlo,
+                                                    nhi, p, nptr, None))
+    return (out, int(n.value)) if want_length else out
+
+
+def nmod_poly_mat_multiply_batch(jobs, ctx: Optional[Context] = None):
+    """jobs: list of (A, B, p) with CUDA tensors; returns the list of products,
+    computed by one pmlg_poly_mat_mul_batch call."""
+    import torch
+    if not jobs:
+        return []
+    ctx = _ctx(ctx, jobs[0][0])
+    outs = []
+    arr = (PolymatJob * len(jobs))()
+    for i, (A, B, p) in enumerate(jobs):
+        _require_cuda(A, B)
+        r, k, l1 = A.shape
+        _, c, l2 = B.shape
+        o = torch.empty((r, c, l1 + l2 - 1 if l1 and l2 else 0), dtype=torch.int64, device=A.device)
+        outs.append(o)
+        arr[i] = PolymatJob(r, k, c, l1, l2, p, _ptr(A), _ptr(B), _ptr(o))
+    ctx.check(ctx.lib.pmlg_poly_mat_mul_batch(ctx.handle, C.cast(arr, C.c_void_p), len(jobs),
+                                              _stream_ptr(jobs[0][0])))
+    return outs
+
+
+# ---------------------------------------------------------------------------
+# L4: approximant bases
+# ---------------------------------------------------------------------------
+
+def _approx(fn_dev, fn_host, F, order: int, shift, p: int, ctx):
+    m, n, flen = F.shape
+    ctx = _ctx(ctx, F)
+    sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+    ln = C.c_int64(0)
+    cap = order + 1
+    shp = sh.ctypes.data_as(C.POINTER(C.c_int64))
+    if _is_torch(F):
+        import torch
+        _require_cuda(F)
+        out = torch.zeros((m, m, cap), dtype=torch.int64, device=F.device)
+        ctx.check(fn_dev(ctx.handle, _ptr(out), cap, shp, _ptr(F), m, n, flen, order, p, C.byref(ln),
+                         _stream_ptr(F)))
+    else:
+        F = np.ascontiguousarray(F, dtype=np.uint64)
+        out = np.zeros((m, m, cap), dtype=np.uint64)
+        ctx.check(fn_host(ctx.handle, _ptr(out), cap, shp, _ptr(F), m, n, flen, order, p, C.byref(ln), None))
+    L = max(int(ln.value), 1)
+    return out[:, :, :L], sh
+
+
+def nmod_poly_mat_pmbasis(F, order: int, shift, p: int, ctx: Optional[Context] = None):
+    """(appbas, shifted row degree) = nmod_poly_mat_pmbasis(F, order, shift)
+    (approximant_basis.c:33).  appbas has shape (m, m, length)."""
+    ctx = _ctx(ctx, F)
+    return _approx(ctx.lib.pmlg_pmbasis, ctx.lib.pmlg_pmbasis_host, F, order, shift, p, ctx)
+
+
+def nmod_poly_mat_mbasis(F, order: int, shift, p: int, ctx: Optional[Context] = None):
+    """nmod_poly_mat_mbasis (approximant_basis.c:18), CUDA tensors only."""
+    ctx = _ctx(ctx, F)
+    return _approx(ctx.lib.pmlg_mbasis, None, F, order, shift, p, ctx)
+
+
+# ---------------------------------------------------------------------------
+# L1: dot products, CRT
+# ---------------------------------------------------------------------------
+
+def nmod_vec_dot_product(v1, v2, p: int, ctx: Optional[Context] = None) -> int:
+    """sum v1[i]*v2[i] mod p, 64-bit entries (nmod_vec_dot_product_unbalanced)."""
+    import torch
+    _require_cuda(v1, v2)
+    ctx = _ctx(ctx, v1)
+    res = torch.zeros(1, dtype=torch.int64, device=v1.device)
+    ctx.check(ctx.lib.pmlg_nmod_vec_dot(ctx.handle, _ptr(res), _ptr(v1), _ptr(v2), v1.numel(), p, _stream_ptr(v1)))
+    return int(res.item()) & (2**64 - 1)
+
+
+def nmod32_vec_dot_product(v1, v2, p: int, ctx: Optional[Context] = None) -> int:
+    """_nmod32_vec_dot_split: 32-bit entries (torch.int32 CUDA tensors)."""
+    import torch
+    _require_cuda(v1, v2)
+    ctx = _ctx(ctx, v1)
+    res = torch.zeros(1, dtype=torch.int32, device=v1.device)
+    ctx.check(ctx.lib.pmlg_nmod32_vec_dot(ctx.handle, _ptr(res), _ptr(v1), _ptr(v2), v1.numel(), p,
+                                          _stream_ptr(v1)))
+    return int(res.item()) & 0xffffffff
+
+
+def nmod32_vec_mdot(mat, vec, p: int, ctx: Optional[Context] = None):
+    """_nmod32_vec_mdot_split: mv[i] = sum_j mat[i, j] vec[j] mod p."""
+    import torch
+    _require_cuda(mat, vec)
+    ctx = _ctx(ctx, mat)
+    nrows, stride = mat.shape
+    out = torch.empty(nrows, dtype=torch.int32, device=mat.device)
+    ctx.check(ctx.lib.pmlg_nmod32_vec_mdot(ctx.handle, _ptr(out), _ptr(mat), _ptr(vec), nrows, vec.numel(), stride,
+                                           p, _stream_ptr(mat)))
+    return out
+
+
+def nmod_vec_dot_product_multi(u, v, p: int, ctx: Optional[Context] = None):
+    """nmod_vec_dot_product_multi: uv[j] = sum_i u[i] v[i, j] mod p."""
+    import torch
+    _require_cuda(u, v)
+    ctx = _ctx(ctx, u)
+    ln, k = v.shape
+    out = torch.empty(k, dtype=torch.int64, device=u.device)
+    ctx.check(ctx.lib.pmlg_nmod_vec_dot_multi(ctx.handle, _ptr(out), _ptr(u), _ptr(v), ln, k, p, _stream_ptr(u)))
+    return out
+
+
+def nmod_multimod_CRT_reduce(x, primes, ctx: Optional[Context] = None):
+    """residues[j] = x mod primes[j] (nmod_multimod_CRT_reduce)."""
+    import torch
+    _require_cuda(x)
+    ctx = _ctx(ctx, x)
+    pr = np.ascontiguousarray(primes, dtype=np.uint64)
+    out = torch.empty((len(pr), x.numel()), dtype=torch.int64, device=x.device)
+    ctx.check(ctx.lib.pmlg_multimod_reduce(ctx.handle, _ptr(out), _ptr(x), x.numel(), pr.ctypes.data, len(pr),
+                                           _stream_ptr(x)))
+    return out
+
+
+def nmod_multimod_CRT_CRT(residues, primes, p: int, ctx: Optional[Context] = None):
+    """out = CRT(residues) mod p (nmod_multimod_CRT_CRT)."""
+    import torch
+    _require_cuda(residues)
+    ctx = _ctx(ctx, residues)
+    pr = np.ascontiguousarray(primes, dtype=np.uint64)
+    nb = residues.shape[1]
+    out = torch.empty(nb, dtype=torch.int64, device=residues.device)
+    ctx.check(ctx.lib.pmlg_multimod_crt(ctx.handle, _ptr(out), _ptr(residues), nb, pr.ctypes.data, len(pr), p,
+                                        _stream_ptr(residues)))
+    return out

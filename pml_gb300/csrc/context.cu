@@ -1,0 +1,410 @@
+// context.cu -- context, scratch memory, NTT tables and CRT plans.
+#include "pmlg_internal.cuh"
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+namespace pmlg {
+
+void set_error(pmlg_ctx *ctx, const char *fmt, ...)
+{
+    if (!ctx)
+        return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(ctx->last_error, sizeof(ctx->last_error), fmt, ap);
+    va_end(ap);
+}
+
+typedef unsigned __int128 u128;
+
+uint64_t h_mulmod(uint64_t a, uint64_t b, uint64_t p) { return (uint64_t)(((u128)a * b) % p); }
+
+uint64_t h_powmod(uint64_t a, uint64_t e, uint64_t p)
+{
+    uint64_t r = 1 % p;
+    a %= p;
+    while (e) {
+        if (e & 1) r = h_mulmod(r, a, p);
+        a = h_mulmod(a, a, p);
+        e >>= 1;
+    }
+    return r;
+}
+
+uint64_t h_invmod(uint64_t a, uint64_t p)
+{
+    __int128 t = 0, nt = 1, r = p, nr = a % p;
+    while (nr != 0) {
+        __int128 qq = r / nr, tmp;
+        tmp = t - qq * nt; t = nt; nt = tmp;
+        tmp = r - qq * nr; r = nr; nr = tmp;
+    }
+    if (r != 1) return 0;
+    if (t < 0) t += p;
+    return (uint64_t)t;
+}
+
+bool h_is_prime(uint64_t n)
+{
+    if (n < 2) return false;
+    static const uint64_t small[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+    for (uint64_t s : small) {
+        if (n == s) return true;
+        if (n % s == 0) return false;
+    }
+    uint64_t d = n - 1;
+    int s = 0;
+    while ((d & 1) == 0) { d >>= 1; s++; }
+    for (uint64_t a : small) {
+        uint64_t x = h_powmod(a, d, n);
+        if (x == 1 || x == n - 1) continue;
+        bool comp = true;
+        for (int r = 1; r < s; r++) {
+            x = h_mulmod(x, x, n);
+            if (x == n - 1) { comp = false; break; }
+        }
+        if (comp) return false;
+    }
+    return true;
+}
+
+// generator of (Z/qZ)^*, q prime
+static uint64_t primitive_root(uint64_t q)
+{
+    uint64_t pm1 = q - 1, fac[64];
+    int nf = 0;
+    uint64_t t = pm1;
+    for (uint64_t f = 2; f * f <= t; f++)
+        if (t % f == 0) { fac[nf++] = f; while (t % f == 0) t /= f; }
+    if (t > 1) fac[nf++] = t;
+    for (uint64_t g = 2;; g++) {
+        bool ok = true;
+        for (int i = 0; i < nf; i++)
+            if (h_powmod(g, pm1 / fac[i], q) == 1) { ok = false; break; }
+        if (ok) return g;
+    }
+}
+
+int get_table(pmlg_ctx *ctx, uint32_t q, int lg, const NttTable **out)
+{
+    for (int i = 0; i < ctx->ntables; i++)
+        if (ctx->tables[i].q == q && ctx->tables[i].lg == lg) {
+            *out = &ctx->tables[i];
+            return PMLG_OK;
+        }
+    if (ctx->ntables >= pmlg_ctx::kMaxTables) {
+        set_error(ctx, "NTT table cache full");
+        return PMLG_ENOMEM;
+    }
+    const uint64_t N = 1ull << lg;
+    if (q >= (1u << 30) || ((uint64_t)q - 1) % N != 0) {
+        set_error(ctx, "q=%u has no root of unity of order 2^%d", q, lg);
+        return PMLG_ENOROOT;
+    }
+    const uint64_t g = primitive_root(q);
+    const uint64_t wN = h_powmod(g, (q - 1) / N, q);
+    const uint64_t iwN = h_invmod(wN, q);
+    uint32_t *hw = (uint32_t *)malloc(4 * N * sizeof(uint32_t));
+    if (!hw) return PMLG_ENOMEM;
+    // interleaved {w, w'} pairs: forward table in [0, 2N), inverse in [2N, 4N)
+    uint32_t *hf = hw, *hi = hw + 2 * N;
+    hf[0] = hi[0] = 1;
+    hf[1] = hi[1] = h_shoup_q(1, q);
+    for (uint64_t h = 1; h < N; h <<= 1) {
+        const uint64_t wh = h_powmod(wN, N / (2 * h), q);
+        const uint64_t iwh = h_powmod(iwN, N / (2 * h), q);
+        uint64_t x = 1, y = 1;
+        for (uint64_t j = 0; j < h; j++) {
+            hf[2 * (h + j)] = (uint32_t)x; hf[2 * (h + j) + 1] = h_shoup_q((uint32_t)x, q);
+            hi[2 * (h + j)] = (uint32_t)y; hi[2 * (h + j) + 1] = h_shoup_q((uint32_t)y, q);
+            x = h_mulmod(x, wh, q);
+            y = h_mulmod(y, iwh, q);
+        }
+    }
+    // exact check of every Shoup quotient: w' * q <= w * 2^32 < (w' + 1) * q
+    for (uint64_t i = 0; i < 2 * N; i++) {
+        const uint32_t w = hw[2 * i], wq = hw[2 * i + 1];
+        const u128 lhs = (u128)wq * q, rhs = (u128)w << 32;
+        if (!(w < q && lhs <= rhs && rhs < lhs + q)) {
+            free(hw);
+            set_error(ctx, "Shoup quotient check failed");
+            return PMLG_EINVAL;
+        }
+    }
+    NttTable T;
+    T.q = q;
+    T.lg = lg;
+    void *d = nullptr;
+    cudaError_t e = cudaMalloc(&d, 4 * N * sizeof(uint32_t));
+    if (e != cudaSuccess) {
+        free(hw);
+        set_error(ctx, "cudaMalloc tables: %s", cudaGetErrorString(e));
+        return PMLG_ENOMEM;
+    }
+    e = cudaMemcpy(d, hw, 4 * N * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    free(hw);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        set_error(ctx, "cudaMemcpy tables: %s", cudaGetErrorString(e));
+        return PMLG_ECUDA;
+    }
+    T.d_w = (uint2 *)d;
+    T.d_iw = T.d_w + N;
+    T.ninv = (uint32_t)h_invmod(N % q, q);
+    T.ninvq = h_shoup_q(T.ninv, q);
+    T.r32 = (uint32_t)((1ull << 32) % q);
+    T.r32q = h_shoup_q(T.r32, q);
+    T.oneq = (uint32_t)((1ull << 32) / q);
+    ctx->tables[ctx->ntables] = T;
+    *out = &ctx->tables[ctx->ntables];
+    ctx->ntables++;
+    return PMLG_OK;
+}
+
+// 30-bit primes q = c * 2^e + 1 with e >= 21, largest first
+static const uint32_t kCrtPrimes[] = {1012924417u, 1004535809u, 998244353u, 985661441u,
+                                      975175681u, 962592769u, 950009857u, 943718401u};
+
+int make_plan(pmlg_ctx *ctx, uint64_t p, int lg, int64_t inner, int64_t minlen, CrtPlan *plan)
+{
+    memset(plan, 0, sizeof(*plan));
+    plan->p = p;
+    if (p < 2) {
+        set_error(ctx, "modulus %llu < 2", (unsigned long long)p);
+        return PMLG_EBADMOD;
+    }
+    if (p < (1ull << 30) && ((p - 1) >> lg) << lg == p - 1 && h_is_prime(p)) {
+        plan->t = 1;
+        plan->q[0] = (uint32_t)p;
+        plan->qp[0] = 0;
+        return PMLG_OK;
+    }
+    if (lg > 21) {
+        set_error(ctx, "transform length 2^%d too large for the CRT primes", lg);
+        return PMLG_ELEN;
+    }
+    // bits of the bound inner * minlen * (p-1)^2 (strictly below 2^bits)
+    u128 pm1 = p - 1;
+    double bits = 0;
+    {
+        // exact enough: compute log2 of each factor with integer bit lengths + 1
+        auto blen = [](u128 x) { int b = 0; while (x) { b++; x >>= 1; } return b; };
+        bits = 2.0 * blen(pm1) + blen((u128)(inner > 0 ? inner : 1)) + blen((u128)(minlen > 0 ? minlen : 1));
+    }
+    // each prime contributes more than 29.8 bits; require strictly more bits than the bound
+    int t = 0;
+    double have = 0;
+    const int navail = (int)(sizeof(kCrtPrimes) / sizeof(kCrtPrimes[0]));
+    while (have <= bits && t < navail) {
+        // log2(q) >= 29.8 for all listed primes
+        have += 29.8;
+        t++;
+    }
+    if (have <= bits || t > kMaxPrimes) {
+        set_error(ctx, "modulus too large for %d CRT primes", kMaxPrimes);
+        return PMLG_EBADMOD;
+    }
+    plan->t = t;
+    for (int j = 0; j < t; j++) plan->q[j] = kCrtPrimes[j];
+    for (int j = 0; j < t; j++) {
+        const uint32_t qj = plan->q[j];
+        uint64_t pr = 1;
+        for (int l = 0; l < j; l++) {
+            plan->qmod[j][l] = plan->q[l] % qj;
+            plan->qmodq[j][l] = h_shoup_q(plan->qmod[j][l], qj);
+            pr = h_mulmod(pr, plan->q[l] % qj, qj);
+        }
+        plan->ginv[j] = (j == 0) ? 1 : (uint32_t)h_invmod(pr, qj);
+        plan->ginvq[j] = h_shoup_q(plan->ginv[j], qj);
+        plan->qp[j] = plan->q[j] % p;
+    }
+    return PMLG_OK;
+}
+
+int ws_reserve(pmlg_ctx *ctx, Workspace *ws, size_t bytes)
+{
+    if (ws->bytes >= bytes)
+        return PMLG_OK;
+    if (ws->ptr) {
+        // the old buffer may still be in use by queued work on any stream
+        cudaError_t e = cudaDeviceSynchronize();
+        if (e != cudaSuccess) {
+            set_error(ctx, "sync before scratch growth: %s", cudaGetErrorString(e));
+            return PMLG_ECUDA;
+        }
+        cudaFree(ws->ptr);
+        ws->ptr = nullptr;
+        ws->bytes = 0;
+    }
+    size_t sz = bytes + (bytes >> 3) + 256;
+    cudaError_t e = cudaMalloc(&ws->ptr, sz);
+    if (e != cudaSuccess) {
+        ws->ptr = nullptr;
+        set_error(ctx, "cudaMalloc scratch (%zu bytes): %s", sz, cudaGetErrorString(e));
+        return PMLG_ENOMEM;
+    }
+    ws->bytes = sz;
+    return PMLG_OK;
+}
+
+static cudaEvent_t pool_event(pmlg_ctx *ctx)
+{
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+void prof_begin(pmlg_ctx *ctx, const char *name, cudaStream_t st)
+{
+    if (!ctx->profiling) return;
+    ProfRecord r{name, pool_event(ctx), pool_event(ctx)};
+    cudaEventRecord(r.beg, st);
+    ctx->prof.push_back(r);
+}
+
+void prof_end(pmlg_ctx *ctx, cudaStream_t st)
+{
+    if (!ctx->profiling || ctx->prof.empty()) return;
+    cudaEventRecord(ctx->prof.back().end, st);
+}
+
+}  // namespace pmlg
+
+using namespace pmlg;
+
+extern "C" {
+
+PMLG_API int pmlg_ctx_create(pmlg_ctx **out, int device)
+{
+    if (!out) return PMLG_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PMLG_ECUDA;
+    if (device < 0 || device >= ndev) return PMLG_EINVAL;
+    pmlg_ctx *ctx = new (std::nothrow) pmlg_ctx();
+    if (!ctx) return PMLG_ENOMEM;
+    ctx->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return PMLG_ECUDA; }
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    *out = ctx;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
+{
+    if (!ctx) return PMLG_OK;
+    cudaSetDevice(ctx->device);
+    cudaDeviceSynchronize();
+    for (int i = 0; i < ctx->ntables; i++) cudaFree(ctx->tables[i].d_w);
+    if (ctx->ws.ptr) cudaFree(ctx->ws.ptr);
+    if (ctx->ws_aux.ptr) cudaFree(ctx->ws_aux.ptr);
+    if (ctx->ws_pm.ptr) cudaFree(ctx->ws_pm.ptr);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    for (auto &r : ctx->prof) { cudaEventDestroy(r.beg); cudaEventDestroy(r.end); }
+    for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    delete ctx;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_set_form(pmlg_ctx *ctx, int form)
+{
+    if (!ctx || form < PMLG_FORM_AUTO || form > PMLG_FORM_INT8_TC) return PMLG_EINVAL;
+    ctx->form = form;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_set_leaf_order(pmlg_ctx *ctx, int64_t order)
+{
+    if (!ctx || order < 0) return PMLG_EINVAL;
+    ctx->leaf_order = order;
+    return PMLG_OK;
+}
+
+PMLG_API unsigned long long pmlg_ctx_launch_count(const pmlg_ctx *ctx)
+{
+    return ctx ? ctx->launches : 0ull;
+}
+
+PMLG_API int pmlg_ctx_set_profiling(pmlg_ctx *ctx, int on)
+{
+    if (!ctx) return PMLG_EINVAL;
+    cudaSetDevice(ctx->device);
+    for (auto &r : ctx->prof) {
+        ctx->event_pool.push_back(r.beg);
+        ctx->event_pool.push_back(r.end);
+    }
+    ctx->prof.clear();
+    ctx->profiling = on ? 1 : 0;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_profile_read(pmlg_ctx *ctx, char *names, size_t names_len, double *ms,
+                                   unsigned long long *counts, int max_kernels, int *n_out)
+{
+    if (!ctx || !n_out || (max_kernels > 0 && (!ms || !counts))) return PMLG_EINVAL;
+    cudaSetDevice(ctx->device);
+    std::vector<const char *> keys;
+    std::vector<double> tot;
+    std::vector<unsigned long long> cnt;
+    for (auto &r : ctx->prof) {
+        if (cudaEventSynchronize(r.end) != cudaSuccess) return PMLG_ECUDA;
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, r.beg, r.end) != cudaSuccess) return PMLG_ECUDA;
+        size_t i = 0;
+        while (i < keys.size() && strcmp(keys[i], r.name) != 0) i++;
+        if (i == keys.size()) { keys.push_back(r.name); tot.push_back(0); cnt.push_back(0); }
+        tot[i] += t;
+        cnt[i] += 1;
+    }
+    const int n = (int)keys.size() < max_kernels ? (int)keys.size() : max_kernels;
+    size_t pos = 0;
+    if (names && names_len) names[0] = 0;
+    for (int i = 0; i < n; i++) {
+        ms[i] = tot[i];
+        counts[i] = cnt[i];
+        if (names) {
+            const size_t l = strlen(keys[i]);
+            if (pos + l + 2 <= names_len) {
+                memcpy(names + pos, keys[i], l);
+                pos += l;
+                names[pos++] = '\n';
+                names[pos] = 0;
+            }
+        }
+    }
+    *n_out = n;
+    return PMLG_OK;
+}
+
+PMLG_API const char *pmlg_ctx_last_error(const pmlg_ctx *ctx)
+{
+    return ctx ? ctx->last_error : "null context";
+}
+
+PMLG_API const char *pmlg_strerror(int status)
+{
+    switch (status) {
+    case PMLG_OK: return "ok";
+    case PMLG_EINVAL: return "invalid argument";
+    case PMLG_EBADMOD: return "unsupported modulus";
+    case PMLG_ENOROOT: return "no root of unity of the needed order";
+    case PMLG_ELEN: return "length beyond the supported transform size";
+    case PMLG_EALIAS: return "output overlaps an input";
+    case PMLG_ETIMEOUT: return "bounded device wait gave up";
+    case PMLG_ECUDA: return "CUDA runtime error";
+    case PMLG_ENOMEM: return "allocation failed";
+    case PMLG_EUNSUP: return "unsupported shape";
+    default: return "unknown status";
+    }
+}
+
+}  // extern "C"

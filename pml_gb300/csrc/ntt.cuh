@@ -1,0 +1,59 @@
+// ntt.cuh -- forward / inverse number-theoretic transforms over 30-bit primes.
+#pragma once
+#include "pmlg_internal.cuh"
+
+namespace pmlg {
+
+// Largest transform handled by one CTA (16 residues per thread, 1024 threads).
+constexpr int kMaxLgN = 14;
+constexpr int kMinLgN = 4;
+
+// Device view of one NttTable.
+struct NttDev
+{
+    const uint2 *w;      // forward or inverse twiddles (by kernel)
+    uint32_t q, ninv, ninvq, r32, r32q, oneq;
+};
+
+// Evaluations are stored "point-tiled": for prime j, point t and matrix entry e,
+//   E[j * prime_stride + (t / 4) * tile_stride + e * 4 + (t % 4)],
+// tile_stride = 4 * (number of entries), so that the four consecutive points
+// of one entry are one 16-byte word and all entries of a 4-point tile are
+// contiguous.  Point t holds the evaluation at w^bitrev(t).
+constexpr int kPtTile = 4;
+
+struct NttFwdArgs
+{
+    const uint64_t *in;     // entry e starts at in + e * in_ld + in_off
+    int64_t in_ld, in_off, L;   // L coefficients are read, the rest is zero
+    int64_t nent;
+    uint32_t *out;
+    int64_t prime_stride, tile_stride;
+    int lg, t, reduce;      // reduce: inputs are < 2^64 and need reduction mod q
+    NttDev tab[kMaxPrimes];
+};
+
+struct NttInvArgs
+{
+    const uint32_t *in;     // point-tiled evaluations
+    int64_t prime_stride, tile_stride;
+    int64_t nent;
+    int64_t lo, cnt;        // coefficients [lo, lo + cnt) of the length-N cyclic result
+    // direct output (t == 1): out64[e * out_ld + d], d < out_cap, zero for d >= cnt
+    uint64_t *out64;
+    int64_t out_ld, out_cap;
+    // CRT output (t > 1): res32[(j * nent + e) * cnt + d]
+    uint32_t *res32;
+    int lg, t;
+    NttDev tab[kMaxPrimes];
+};
+
+int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a, cudaStream_t st);
+int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st);
+
+// out64[e * out_ld + d] = CRT(res32[(j * nent + e) * cnt + d], j < t) mod p for
+// d < cnt; zero for cnt <= d < out_cap.
+int crt_combine(pmlg_ctx *ctx, const CrtPlan &plan, const uint32_t *res32, int64_t nent,
+                int64_t cnt, uint64_t *out64, int64_t out_ld, int64_t out_cap, cudaStream_t st);
+
+}  // namespace pmlg

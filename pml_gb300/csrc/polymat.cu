@@ -1,0 +1,379 @@
+// polymat.cu -- nmod_poly_mat_multiply / mulmid on the GPU:
+// forward NTT of every entry -> pointwise matrix products at the N points ->
+// inverse NTT (+ CRT when the modulus is not an NTT prime).
+//
+// The reference evaluates at a geometric progression (FLINT
+// _nmod_poly_evaluate_geometric_nmod_vec_fast_precomp, mul_geometric.c:78,89)
+// and interpolates (mul_geometric.c:104); evaluating at 2^lg-th roots of unity
+// gives the same unique product mod p.  Middle products use the cyclic
+// wrap-around of a length-N transform: with N >= nhi and N >= len1+len2-1-nlo,
+// the coefficients [nlo, nhi) of the cyclic product equal those of the full one.
+#include "polymat.cuh"
+#include "ntt.cuh"
+#include "pointwise.cuh"
+
+#include <cstring>
+
+namespace pmlg {
+
+int lg_for(int64_t n)
+{
+    int lg = kMinLgN;
+    while ((1ll << lg) < n) lg++;
+    return lg;
+}
+
+static inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t product_scratch_bytes(const ProductJob &j, const CrtPlan &plan)
+{
+    const size_t N = (size_t)1 << j.lg, t = plan.t;
+    size_t b = 0;
+    b += align256(t * N * j.r * j.k * 4);
+    b += align256(t * N * j.k * j.c * 4);
+    b += align256(t * N * j.r * j.c * 4);
+    if (t > 1) b += align256(t * j.r * j.c * j.cnt * 4);
+    return b;
+}
+
+int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch, int form,
+                cudaStream_t st)
+{
+    const int64_t N = 1ll << j.lg;
+    const int t = plan.t;
+    const int64_t nA = j.r * j.k, nB = j.k * j.c, nC = j.r * j.c;
+    char *w = (char *)scratch;
+    uint32_t *EA = (uint32_t *)w; w += align256((size_t)t * N * nA * 4);
+    uint32_t *EB = (uint32_t *)w; w += align256((size_t)t * N * nB * 4);
+    uint32_t *EC = (uint32_t *)w; w += align256((size_t)t * N * nC * 4);
+    uint32_t *R32 = (t > 1) ? (uint32_t *)w : nullptr;
+
+    const NttTable *tabs[kMaxPrimes];
+    for (int i = 0; i < t; i++) PMLG_TRY(get_table(ctx, plan.q[i], j.lg, &tabs[i]));
+
+    NttFwdArgs fa{};
+    fa.lg = j.lg;
+    fa.t = t;
+    fa.reduce = (t > 1);
+    for (int i = 0; i < t; i++)
+        fa.tab[i] = NttDev{tabs[i]->d_w, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
+                           tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
+    // A
+    fa.in = j.A; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = nA;
+    fa.out = EA; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
+    PMLG_TRY(ntt_forward(ctx, fa, st));
+    // B
+    fa.in = j.B; fa.in_ld = j.ldb; fa.in_off = j.b_off; fa.L = j.b_len; fa.nent = nB;
+    fa.out = EB; fa.prime_stride = N * nB; fa.tile_stride = kPtTile * nB;
+    PMLG_TRY(ntt_forward(ctx, fa, st));
+
+    // pointwise products, one prime at a time
+    for (int i = 0; i < t; i++) {
+        PwArgs pa{};
+        pa.A = {EA + (size_t)i * N * nA, kPtTile * nA, j.k};
+        pa.B = {EB + (size_t)i * N * nB, kPtTile * nB, j.c};
+        pa.C = EC + (size_t)i * N * nC;
+        pa.s_tile_c = kPtTile * nC;
+        pa.ldc = j.c;
+        pa.pt_tile = kPtTile;
+        pa.s_e = kPtTile;
+        pa.s_p = 1;
+        pa.npts = N;
+        pa.accumulate = 0;
+        pointwise_set_modulus(pa, plan.q[i]);
+        PMLG_TRY(pointwise_blocked(ctx, pa, j.r, j.k, j.c, form, st));
+    }
+
+    NttInvArgs ia{};
+    ia.in = EC; ia.prime_stride = N * nC; ia.tile_stride = kPtTile * nC; ia.nent = nC;
+    ia.lo = j.lo; ia.cnt = j.cnt;
+    ia.out64 = j.C; ia.out_ld = j.ldc; ia.out_cap = j.c_cap;
+    ia.res32 = R32;
+    ia.lg = j.lg; ia.t = t;
+    for (int i = 0; i < t; i++)
+        ia.tab[i] = NttDev{tabs[i]->d_iw, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
+                           tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
+    PMLG_TRY(ntt_inverse(ctx, ia, st));
+    if (t > 1) PMLG_TRY(crt_combine(ctx, plan, R32, nC, j.cnt, j.C, j.ldc, j.c_cap, st));
+    return PMLG_OK;
+}
+
+int mulmid_prepare(ProductJob &j, int64_t len1, int64_t len2, int64_t nlo, int64_t nhi)
+{
+    int64_t a_len = len1 < nhi ? len1 : nhi;
+    int64_t b_len = len2 < nhi ? len2 : nhi;
+    int64_t a_off = 0, b_off = 0, lo = nlo;
+    int64_t hi = nhi;
+    if (hi > a_len + b_len - 1) hi = a_len + b_len - 1;
+    if (a_len <= 0 || b_len <= 0 || hi <= lo) {
+        j.cnt = 0;
+        return 0;
+    }
+    // coefficients of B below lo - (a_len - 1) only reach product terms below lo
+    int64_t sB = lo - (a_len - 1);
+    if (sB > 0) { b_off += sB; b_len -= sB; lo -= sB; hi -= sB; }
+    int64_t sA = lo - (b_len - 1);
+    if (sA > 0) { a_off += sA; a_len -= sA; lo -= sA; hi -= sA; }
+    j.a_off = a_off; j.a_len = a_len;
+    j.b_off = b_off; j.b_len = b_len;
+    j.lo = lo;
+    j.cnt = hi - lo;
+    int64_t need = hi;
+    if (a_len + b_len - 1 - lo > need) need = a_len + b_len - 1 - lo;
+    j.lg = lg_for(need);
+    return j.lg;
+}
+
+// ---------------------------------------------------------------------------
+// max length of a polynomial matrix (device), for the clamped lengths
+// ---------------------------------------------------------------------------
+
+__global__ void maxlen_kernel(const uint64_t *__restrict__ P, int64_t nent, int64_t ld, int64_t len,
+                              unsigned long long *out)
+{
+    const int64_t total = nent * len;
+    unsigned long long best = 0;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = idx / len, d = idx - e * len;
+        if (P[e * ld + d] != 0 && (unsigned long long)(d + 1) > best) best = d + 1;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long v = __shfl_down_sync(0xffffffffu, best, o);
+        best = v > best ? v : best;
+    }
+    if ((threadIdx.x & 31) == 0 && best) atomicMax(out, best);
+}
+
+int device_max_length(pmlg_ctx *ctx, const uint64_t *P, int64_t nent, int64_t ld, int64_t len,
+                      unsigned long long *d_tmp, int64_t *out, cudaStream_t st)
+{
+    PMLG_CUDA_TRY(cudaMemsetAsync(d_tmp, 0, sizeof(unsigned long long), st));
+    if (nent > 0 && len > 0) {
+        int64_t blocks = (nent * len + 255) / 256;
+        if (blocks > (int64_t)ctx->sm_count * 8) blocks = (int64_t)ctx->sm_count * 8;
+        prof_begin(ctx, "maxlen", st);
+        maxlen_kernel<<<(unsigned)blocks, 256, 0, st>>>(P, nent, ld, len, d_tmp);
+        prof_end(ctx, st);
+        count_launch(ctx);
+        PMLG_CUDA_TRY(cudaGetLastError());
+    }
+    unsigned long long h = 0;
+    PMLG_CUDA_TRY(cudaMemcpyAsync(&h, d_tmp, sizeof(h), cudaMemcpyDeviceToHost, st));
+    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    *out = (int64_t)h;
+    return PMLG_OK;
+}
+
+static bool overlaps(const void *a, size_t na, const void *b, size_t nb)
+{
+    const char *x = (const char *)a, *y = (const char *)b;
+    return na && nb && x < y + nb && y < x + na;
+}
+
+// ---------------------------------------------------------------------------
+// entry points
+// ---------------------------------------------------------------------------
+
+static int run_job_alloc(pmlg_ctx *ctx, const ProductJob &j, cudaStream_t st)
+{
+    CrtPlan plan;
+    const int64_t minlen = j.a_len < j.b_len ? j.a_len : j.b_len;
+    PMLG_TRY(make_plan(ctx, j.p, j.lg, j.k, minlen, &plan));
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan)));
+    return product_run(ctx, j, plan, ctx->ws.ptr, ctx->form, st);
+}
+
+int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B, int64_t r,
+                        int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p, cudaStream_t st)
+{
+    const int64_t clen = (len1 > 0 && len2 > 0) ? len1 + len2 - 1 : 0;
+    if (r == 0 || c == 0 || clen == 0) return PMLG_OK;
+    if (k == 0) {
+        PMLG_CUDA_TRY(cudaMemsetAsync(C, 0, (size_t)(r * c * clen) * 8, st));
+        return PMLG_OK;
+    }
+    ProductJob j{};
+    j.r = r; j.k = k; j.c = c;
+    j.A = A; j.lda = len1; j.a_off = 0; j.a_len = len1;
+    j.B = B; j.ldb = len2; j.b_off = 0; j.b_len = len2;
+    j.C = C; j.ldc = clen; j.c_cap = clen;
+    j.lo = 0; j.cnt = clen;
+    j.lg = lg_for(clen);
+    j.p = p;
+    if (j.lg > kMaxLgN) {
+        set_error(ctx, "product length %lld needs a transform beyond 2^%d", (long long)clen, kMaxLgN);
+        return PMLG_ELEN;
+    }
+    return run_job_alloc(ctx, j, st);
+}
+
+int poly_mat_mulmid_device(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, const uint64_t *B,
+                           int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2, int64_t nlo,
+                           int64_t nhi, uint64_t p, cudaStream_t st)
+{
+    const int64_t cap = nhi - nlo;
+    if (cap <= 0 || r == 0 || c == 0) return PMLG_OK;
+    ProductJob j{};
+    j.r = r; j.k = k; j.c = c;
+    j.A = A; j.lda = len1;
+    j.B = B; j.ldb = len2;
+    j.C = res; j.ldc = cap; j.c_cap = cap;
+    j.p = p;
+    mulmid_prepare(j, k == 0 ? 0 : len1, len2, nlo, nhi);
+    if (j.cnt <= 0) {
+        PMLG_CUDA_TRY(cudaMemsetAsync(res, 0, (size_t)(r * c * cap) * 8, st));
+        return PMLG_OK;
+    }
+    if (j.lg > kMaxLgN) {
+        set_error(ctx, "middle product needs a transform beyond 2^%d", kMaxLgN);
+        return PMLG_ELEN;
+    }
+    return run_job_alloc(ctx, j, st);
+}
+
+static int check_common(pmlg_ctx *ctx, const void *C, const void *A, const void *B, int64_t r, int64_t k,
+                        int64_t c, int64_t len1, int64_t len2, uint64_t p)
+{
+    if (!ctx) return PMLG_EINVAL;
+    if (r < 0 || k < 0 || c < 0 || len1 < 0 || len2 < 0) return PMLG_EINVAL;
+    if (p < 2) { set_error(ctx, "modulus must be >= 2"); return PMLG_EBADMOD; }
+    if ((r * k * len1 > 0 && !A) || (k * c * len2 > 0 && !B) || (r * c > 0 && !C)) return PMLG_EINVAL;
+    return PMLG_OK;
+}
+
+// host -> device copy on the stream (asynchronous when the source is pinned)
+static int h2d(pmlg_ctx *ctx, void *dst, const void *src, size_t bytes, cudaStream_t st)
+{
+    if (!bytes) return PMLG_OK;
+    PMLG_CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+    return PMLG_OK;
+}
+
+}  // namespace pmlg
+
+using namespace pmlg;
+
+extern "C" {
+
+PMLG_API int pmlg_poly_mat_mul(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B,
+                               int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                               uint64_t p, void *stream)
+{
+    PMLG_TRY(check_common(ctx, C, A, B, r, k, c, len1, len2, p));
+    const int64_t clen = (len1 > 0 && len2 > 0) ? len1 + len2 - 1 : 0;
+    if (overlaps(C, (size_t)(r * c * clen) * 8, A, (size_t)(r * k * len1) * 8) ||
+        overlaps(C, (size_t)(r * c * clen) * 8, B, (size_t)(k * c * len2) * 8)) {
+        set_error(ctx, "output overlaps an input");
+        return PMLG_EALIAS;
+    }
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    return poly_mat_mul_device(ctx, C, A, B, r, k, c, len1, len2, p, (cudaStream_t)stream);
+}
+
+PMLG_API int pmlg_poly_mat_mulmid(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, const uint64_t *B,
+                                  int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                                  int64_t nlo, int64_t nhi, uint64_t p, int64_t *out_len, void *stream)
+{
+    PMLG_TRY(check_common(ctx, res, A, B, r, k, c, len1, len2, p));
+    if (nlo < 0 || nhi < 0) return PMLG_EINVAL;
+    const int64_t cap = nhi > nlo ? nhi - nlo : 0;
+    if (overlaps(res, (size_t)(r * c * cap) * 8, A, (size_t)(r * k * len1) * 8) ||
+        overlaps(res, (size_t)(r * c * cap) * 8, B, (size_t)(k * c * len2) * 8)) {
+        set_error(ctx, "output overlaps an input");
+        return PMLG_EALIAS;
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    PMLG_TRY(poly_mat_mulmid_device(ctx, res, A, B, r, k, c, len1, len2, nlo, nhi, p, st));
+    if (out_len) {
+        // clamp as mulmid.c:505-507 does, with the actual max lengths
+        PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, 256));
+        unsigned long long *tmp = (unsigned long long *)ctx->ws_aux.ptr;
+        int64_t L1 = 0, L2 = 0;
+        PMLG_TRY(device_max_length(ctx, A, r * k, len1, len1, tmp, &L1, st));
+        PMLG_TRY(device_max_length(ctx, B, k * c, len2, len2, tmp, &L2, st));
+        int64_t hi = nhi;
+        if (L1 == 0 || L2 == 0) hi = 0;
+        else if (hi > L1 + L2 - 1) hi = L1 + L2 - 1;
+        *out_len = hi > nlo ? hi - nlo : 0;
+    }
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B,
+                                    int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                                    uint64_t p, void *stream)
+{
+    PMLG_TRY(check_common(ctx, C, A, B, r, k, c, len1, len2, p));
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int64_t clen = (len1 > 0 && len2 > 0) ? len1 + len2 - 1 : 0;
+    const size_t bA = (size_t)(r * k * len1) * 8, bB = (size_t)(k * c * len2) * 8,
+                 bC = (size_t)(r * c * clen) * 8;
+    const size_t oA = 0, oB = (bA + 255) & ~(size_t)255, oC = oB + ((bB + 255) & ~(size_t)255);
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, oC + bC + 256));
+    char *base = (char *)ctx->ws_aux.ptr;
+    uint64_t *dA = (uint64_t *)(base + oA), *dB = (uint64_t *)(base + oB), *dC = (uint64_t *)(base + oC);
+    PMLG_TRY(h2d(ctx, dA, A, bA, st));
+    PMLG_TRY(h2d(ctx, dB, B, bB, st));
+    PMLG_TRY(poly_mat_mul_device(ctx, dC, dA, dB, r, k, c, len1, len2, p, st));
+    if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(C, dC, bC, cudaMemcpyDeviceToHost, st));
+    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_poly_mat_mulmid_host(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A,
+                                       const uint64_t *B, int64_t r, int64_t k, int64_t c,
+                                       int64_t len1, int64_t len2, int64_t nlo, int64_t nhi,
+                                       uint64_t p, int64_t *out_len, void *stream)
+{
+    PMLG_TRY(check_common(ctx, res, A, B, r, k, c, len1, len2, p));
+    if (nlo < 0 || nhi < 0) return PMLG_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int64_t cap = nhi > nlo ? nhi - nlo : 0;
+    const size_t bA = (size_t)(r * k * len1) * 8, bB = (size_t)(k * c * len2) * 8,
+                 bC = (size_t)(r * c * cap) * 8;
+    const size_t oA = 0, oB = (bA + 255) & ~(size_t)255, oC = oB + ((bB + 255) & ~(size_t)255);
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, oC + bC + 512));
+    char *base = (char *)ctx->ws_aux.ptr;
+    uint64_t *dA = (uint64_t *)(base + oA), *dB = (uint64_t *)(base + oB), *dC = (uint64_t *)(base + oC);
+    PMLG_TRY(h2d(ctx, dA, A, bA, st));
+    PMLG_TRY(h2d(ctx, dB, B, bB, st));
+    PMLG_TRY(poly_mat_mulmid_device(ctx, dC, dA, dB, r, k, c, len1, len2, nlo, nhi, p, st));
+    if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(res, dC, bC, cudaMemcpyDeviceToHost, st));
+    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (out_len) {
+        // the actual max lengths are read on the host copies
+        auto hostlen = [](const uint64_t *P, int64_t nent, int64_t len) {
+            int64_t L = 0;
+            for (int64_t e = 0; e < nent; e++)
+                for (int64_t d = len - 1; d >= L; d--)
+                    if (P[e * len + d]) { L = d + 1; break; }
+            return L;
+        };
+        const int64_t L1 = hostlen(A, r * k, len1), L2 = hostlen(B, k * c, len2);
+        int64_t hi = nhi;
+        if (L1 == 0 || L2 == 0) hi = 0;
+        else if (hi > L1 + L2 - 1) hi = L1 + L2 - 1;
+        *out_len = hi > nlo ? hi - nlo : 0;
+    }
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs, int64_t njobs,
+                                     void *stream)
+{
+    if (!ctx || (njobs > 0 && !jobs) || njobs < 0) return PMLG_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    for (int64_t i = 0; i < njobs; i++) {
+        const pmlg_polymat_job &J = jobs[i];
+        PMLG_TRY(check_common(ctx, J.C, J.A, J.B, J.r, J.k, J.c, J.len1, J.len2, J.p));
+        PMLG_TRY(poly_mat_mul_device(ctx, J.C, J.A, J.B, J.r, J.k, J.c, J.len1, J.len2, J.p, st));
+    }
+    return PMLG_OK;
+}
+
+}  // extern "C"

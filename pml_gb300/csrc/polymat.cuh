@@ -1,0 +1,40 @@
+// polymat.cuh -- evaluation / pointwise / interpolation pipeline shared by the
+// product, the middle product, the batched products and pmbasis.
+#pragma once
+#include "pmlg_internal.cuh"
+
+namespace pmlg {
+
+// One product job in device memory.  Coefficients [lo, lo + cnt) of the
+// length-N cyclic convolution of A (entries A + e*lda + a_off, a_len
+// coefficients) and B (likewise) are written to C (entry stride ldc, capacity
+// c_cap, zero beyond cnt).  N = 2^lg must satisfy N >= lo + cnt and
+// N >= a_len + b_len - 1 - lo so that no wrapped term lands in the window.
+struct ProductJob
+{
+    int64_t r, k, c;
+    const uint64_t *A;
+    int64_t lda, a_off, a_len;
+    const uint64_t *B;
+    int64_t ldb, b_off, b_len;
+    uint64_t *C;
+    int64_t ldc, c_cap;
+    int64_t lo, cnt;
+    int lg;
+    uint64_t p;
+};
+
+// Bytes of scratch one job needs.
+size_t product_scratch_bytes(const ProductJob &j, const CrtPlan &plan);
+
+// Runs one job on the stream using `scratch` (at least product_scratch_bytes).
+int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch,
+                int form, cudaStream_t st);
+
+// Transform size for a middle product window after the input trimming of
+// mulmid.c:516-556: returns lg, and adjusts offsets/lengths/window in place.
+int mulmid_prepare(ProductJob &j, int64_t len1, int64_t len2, int64_t nlo, int64_t nhi);
+
+int lg_for(int64_t n);
+
+}  // namespace pmlg

@@ -1,0 +1,388 @@
+// vec.cu -- modular dot products with delayed reduction, multimodular
+// reduction and CRT.
+//
+// Dot products accumulate the exact integer sum (192-bit per thread for 64-bit
+// entries, 128-bit for 32-bit entries), reduce the partial sums across the
+// grid exactly, and reduce mod p once at the end: the same delayed-reduction
+// idea as nmod_vec_dot_product_unbalanced's 3-limb accumulator
+// (flint-extras/src/nmod_vec_extra/nmod_vec_dot_product.c:68-127) and
+// _nmod32_vec_dot_split (nmod32_vec/dot_split.c:18-47), without their length
+// limits.
+#include "pmlg_internal.cuh"
+
+namespace pmlg {
+
+struct U192
+{
+    unsigned long long w0, w1, w2;
+};
+
+__device__ __forceinline__ void add128(U192 &a, unsigned long long lo, unsigned long long hi)
+{
+    // a += hi:lo with carries into w2
+    unsigned long long s0 = a.w0 + lo;
+    unsigned long long c0 = s0 < lo;
+    unsigned long long s1 = a.w1 + hi;
+    unsigned long long c1 = s1 < hi;
+    unsigned long long s1b = s1 + c0;
+    c1 += s1b < c0;
+    a.w0 = s0;
+    a.w1 = s1b;
+    a.w2 += c1;
+}
+
+__device__ __forceinline__ void add192(U192 &a, const U192 &b)
+{
+    add128(a, b.w0, b.w1);
+    a.w2 += b.w2;
+}
+
+__device__ __forceinline__ U192 shfl_down192(const U192 &v, int o)
+{
+    U192 r;
+    r.w0 = __shfl_down_sync(0xffffffffu, v.w0, o);
+    r.w1 = __shfl_down_sync(0xffffffffu, v.w1, o);
+    r.w2 = __shfl_down_sync(0xffffffffu, v.w2, o);
+    return r;
+}
+
+// block-wide exact sum; result valid in thread 0
+__device__ U192 block_sum192(U192 v)
+{
+    __shared__ U192 part[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        U192 w = shfl_down192(v, o);
+        add192(v, w);
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+        v = lane < nw ? part[lane] : U192{0, 0, 0};
+        for (int o = 16; o > 0; o >>= 1) {
+            U192 w = shfl_down192(v, o);
+            add192(v, w);
+        }
+    }
+    return v;
+}
+
+__device__ __forceinline__ uint64_t mod192(const U192 &v, uint64_t p)
+{
+    unsigned __int128 acc = v.w2 % p;
+    acc = ((acc << 64) | v.w1) % p;
+    acc = ((acc << 64) | v.w0) % p;
+    return (uint64_t)acc;
+}
+
+__global__ void dot64_partial(const uint64_t *__restrict__ v1, const uint64_t *__restrict__ v2, int64_t len,
+                              U192 *part)
+{
+    U192 acc{0, 0, 0};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = v1[i], b = v2[i];
+        add128(acc, a * b, __umul64hi(a, b));
+    }
+    acc = block_sum192(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void dot32_partial(const uint32_t *__restrict__ v1, const uint32_t *__restrict__ v2, int64_t len,
+                              U192 *part)
+{
+    // products < 2^64: accumulate in 64 bits and carry into the high words
+    U192 acc{0, 0, 0};
+    const int64_t n4 = len >> 2;
+    const uint4 *a4 = reinterpret_cast<const uint4 *>(v1);
+    const uint4 *b4 = reinterpret_cast<const uint4 *>(v2);
+    const bool vec = ((reinterpret_cast<uintptr_t>(v1) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t start = 0;
+    if (vec) {
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
+            const uint4 a = a4[i], b = b4[i];
+            add128(acc, (uint64_t)a.x * b.x, 0);
+            add128(acc, (uint64_t)a.y * b.y, 0);
+            add128(acc, (uint64_t)a.z * b.z, 0);
+            add128(acc, (uint64_t)a.w * b.w, 0);
+        }
+        start = n4 << 2;
+    }
+    for (int64_t i = start + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
+        add128(acc, (uint64_t)v1[i] * v2[i], 0);
+    acc = block_sum192(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = acc;
+}
+
+__global__ void dot_final(const U192 *part, int nparts, uint64_t p, uint64_t *res64, uint32_t *res32)
+{
+    U192 acc{0, 0, 0};
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) add192(acc, part[i]);
+    acc = block_sum192(acc);
+    if (threadIdx.x == 0) {
+        const uint64_t r = mod192(acc, p);
+        if (res64) *res64 = r;
+        if (res32) *res32 = (uint32_t)r;
+    }
+}
+
+// one warp per row: mv[i] = sum_j mat[i*stride + j] * vec[j] mod p
+__global__ void mdot32_kernel(uint32_t *mv, const uint32_t *__restrict__ mat, const uint32_t *__restrict__ vec,
+                              int64_t nrows, int64_t len, int64_t stride, uint64_t p)
+{
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (warp >= nrows) return;
+    const uint32_t *row = mat + warp * stride;
+    U192 acc{0, 0, 0};
+    for (int64_t j = lane; j < len; j += 32) add128(acc, (uint64_t)row[j] * vec[j], 0);
+    for (int o = 16; o > 0; o >>= 1) {
+        U192 w = shfl_down192(acc, o);
+        add192(acc, w);
+    }
+    if (lane == 0) mv[warp] = (uint32_t)mod192(acc, p);
+}
+
+// uv[j] = sum_i u[i] * v[i*k + j]: grid.x over columns, grid.y over chunks of i
+__global__ void dot_multi_partial(const uint64_t *__restrict__ u, const uint64_t *__restrict__ v, int64_t len,
+                                  int64_t k, int64_t chunk, U192 *part)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k) return;
+    const int64_t i0 = (int64_t)blockIdx.y * chunk;
+    const int64_t i1 = i0 + chunk < len ? i0 + chunk : len;
+    U192 acc{0, 0, 0};
+    for (int64_t i = i0; i < i1; i++) {
+        const uint64_t a = u[i], b = v[i * k + j];
+        add128(acc, a * b, __umul64hi(a, b));
+    }
+    part[(int64_t)blockIdx.y * k + j] = acc;
+}
+
+__global__ void dot_multi_final(const U192 *part, int64_t nchunks, int64_t k, uint64_t p, uint64_t *uv)
+{
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= k) return;
+    U192 acc{0, 0, 0};
+    for (int64_t c = 0; c < nchunks; c++) add192(acc, part[c * k + j]);
+    uv[j] = mod192(acc, p);
+}
+
+// residues[j*nb + i] = x[i] mod q_j; Barrett quotient estimate with m_j = floor((2^64-1)/q_j)
+struct MultimodArgs
+{
+    int t;
+    uint64_t q[kMaxPrimes], m[kMaxPrimes];
+};
+
+__global__ void multimod_reduce_kernel(uint64_t *res, const uint64_t *__restrict__ x, int64_t nb, MultimodArgs a)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t v = x[i];
+        for (int j = 0; j < a.t; j++) {
+            const uint64_t qe = __umul64hi(v, a.m[j]);
+            uint64_t r = v - qe * a.q[j];
+            while (r >= a.q[j]) r -= a.q[j];
+            res[j * nb + i] = r;
+        }
+    }
+}
+
+struct CrtArgs64
+{
+    int t;
+    uint64_t q[kMaxPrimes];
+    uint64_t ginv[kMaxPrimes];         // (q_0 ... q_{j-1})^{-1} mod q_j
+    uint64_t p;
+};
+
+__device__ __forceinline__ uint64_t mulmod64(uint64_t a, uint64_t b, uint64_t m)
+{
+    return (uint64_t)(((unsigned __int128)a * b) % m);
+}
+
+__global__ void multimod_crt_kernel(uint64_t *out, const uint64_t *__restrict__ res, int64_t nb, CrtArgs64 a)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t c[kMaxPrimes];
+        for (int j = 0; j < a.t; j++) {
+            const uint64_t qj = a.q[j];
+            uint64_t v = 0;
+            for (int l = j - 1; l >= 0; l--) v = (mulmod64(v, a.q[l] % qj, qj) + c[l] % qj) % qj;
+            const uint64_t r = res[j * nb + i] % qj;
+            const uint64_t d = r >= v ? r - v : r + (qj - v);
+            c[j] = (j == 0) ? r : mulmod64(d, a.ginv[j], qj);
+        }
+        uint64_t x = 0;
+        for (int l = a.t - 1; l >= 0; l--) {
+            unsigned __int128 y = (unsigned __int128)x * (a.q[l] % a.p) + (c[l] % a.p);
+            x = (uint64_t)(y % a.p);
+        }
+        out[i] = x;
+    }
+}
+
+static int grid_for(pmlg_ctx *ctx, int64_t n, int threads, int per_sm)
+{
+    int64_t b = (n + threads - 1) / threads;
+    const int64_t cap = (int64_t)ctx->sm_count * per_sm;
+    if (b > cap) b = cap;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+}  // namespace pmlg
+
+using namespace pmlg;
+
+extern "C" {
+
+PMLG_API int pmlg_nmod_vec_dot(pmlg_ctx *ctx, uint64_t *res, const uint64_t *v1, const uint64_t *v2,
+                               int64_t len, uint64_t p, void *stream)
+{
+    if (!ctx || !res || len < 0 || (len > 0 && (!v1 || !v2))) return PMLG_EINVAL;
+    if (p < 2) return PMLG_EBADMOD;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int threads = 256;
+    const int blocks = grid_for(ctx, len, threads, 4);
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, sizeof(U192) * (size_t)blocks + 256));
+    U192 *part = (U192 *)ctx->ws_aux.ptr;
+    prof_begin(ctx, "dot64_partial", st);
+    dot64_partial<<<blocks, threads, 0, st>>>(v1, v2, len, part);
+    prof_end(ctx, st);
+    prof_begin(ctx, "dot_final", st);
+    dot_final<<<1, 256, 0, st>>>(part, blocks, p, res, nullptr);
+    prof_end(ctx, st);
+    count_launch(ctx, 2);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_nmod32_vec_dot(pmlg_ctx *ctx, uint32_t *res, const uint32_t *v1, const uint32_t *v2,
+                                 int64_t len, uint64_t p, void *stream)
+{
+    if (!ctx || !res || len < 0 || (len > 0 && (!v1 || !v2))) return PMLG_EINVAL;
+    if (p < 2 || p > (1ull << 32)) return PMLG_EBADMOD;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int threads = 256;
+    const int blocks = grid_for(ctx, (len + 3) / 4, threads, 4);
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, sizeof(U192) * (size_t)blocks + 256));
+    U192 *part = (U192 *)ctx->ws_aux.ptr;
+    prof_begin(ctx, "dot32_partial", st);
+    dot32_partial<<<blocks, threads, 0, st>>>(v1, v2, len, part);
+    prof_end(ctx, st);
+    prof_begin(ctx, "dot_final", st);
+    dot_final<<<1, 256, 0, st>>>(part, blocks, p, nullptr, res);
+    prof_end(ctx, st);
+    count_launch(ctx, 2);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_nmod32_vec_mdot(pmlg_ctx *ctx, uint32_t *mv, const uint32_t *mat, const uint32_t *vec,
+                                  int64_t nrows, int64_t len, int64_t stride, uint64_t p, void *stream)
+{
+    if (!ctx || nrows < 0 || len < 0 || stride < len) return PMLG_EINVAL;
+    if (nrows == 0) return PMLG_OK;
+    if (!mv || (len > 0 && (!mat || !vec))) return PMLG_EINVAL;
+    if (p < 2 || p > (1ull << 32)) return PMLG_EBADMOD;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int threads = 256;
+    const int64_t blocks = (nrows * 32 + threads - 1) / threads;
+    prof_begin(ctx, "mdot32", st);
+    mdot32_kernel<<<(unsigned)blocks, threads, 0, st>>>(mv, mat, vec, nrows, len, stride, p);
+    prof_end(ctx, st);
+    count_launch(ctx);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t *u, const uint64_t *v,
+                                     int64_t len, int64_t k, uint64_t p, void *stream)
+{
+    if (!ctx || len < 0 || k < 0) return PMLG_EINVAL;
+    if (k == 0) return PMLG_OK;
+    if (!uv || (len > 0 && (!u || !v))) return PMLG_EINVAL;
+    if (p < 2) return PMLG_EBADMOD;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const int threads = 128;
+    const int64_t gx = (k + threads - 1) / threads;
+    // enough chunks along i to fill the GPU, each at least 64 rows long
+    int64_t nchunks = ((int64_t)ctx->sm_count * 8 + gx - 1) / gx;
+    if (nchunks > (len + 63) / 64) nchunks = (len + 63) / 64;
+    if (nchunks < 1) nchunks = 1;
+    if (nchunks > 65535) nchunks = 65535;
+    const int64_t chunk = (len + nchunks - 1) / nchunks > 0 ? (len + nchunks - 1) / nchunks : 1;
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, sizeof(U192) * (size_t)(nchunks * k) + 256));
+    U192 *part = (U192 *)ctx->ws_aux.ptr;
+    prof_begin(ctx, "dot_multi_partial", st);
+    dot_multi_partial<<<dim3((unsigned)gx, (unsigned)nchunks), threads, 0, st>>>(u, v, len, k, chunk, part);
+    prof_end(ctx, st);
+    prof_begin(ctx, "dot_multi_final", st);
+    dot_multi_final<<<(unsigned)gx, threads, 0, st>>>(part, nchunks, k, p, uv);
+    prof_end(ctx, st);
+    count_launch(ctx, 2);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_multimod_reduce(pmlg_ctx *ctx, uint64_t *residues, const uint64_t *input, int64_t nb,
+                                  const uint64_t *primes, int nprimes, void *stream)
+{
+    if (!ctx || nb < 0 || !primes || nprimes < 1 || nprimes > kMaxPrimes) return PMLG_EINVAL;
+    if (nb == 0) return PMLG_OK;
+    if (!residues || !input) return PMLG_EINVAL;
+    MultimodArgs a{};
+    a.t = nprimes;
+    for (int j = 0; j < nprimes; j++) {
+        if (primes[j] < 2 || primes[j] >= (1ull << 63)) return PMLG_EBADMOD;
+        a.q[j] = primes[j];
+        a.m[j] = ~0ull / primes[j];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    prof_begin(ctx, "multimod_reduce", st);
+    multimod_reduce_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(residues, input, nb, a);
+    prof_end(ctx, st);
+    count_launch(ctx);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_multimod_crt(pmlg_ctx *ctx, uint64_t *out, const uint64_t *residues, int64_t nb,
+                               const uint64_t *primes, int nprimes, uint64_t p, void *stream)
+{
+    if (!ctx || nb < 0 || !primes || nprimes < 1 || nprimes > kMaxPrimes) return PMLG_EINVAL;
+    if (p < 2) return PMLG_EBADMOD;
+    if (nb == 0) return PMLG_OK;
+    if (!out || !residues) return PMLG_EINVAL;
+    CrtArgs64 a{};
+    a.t = nprimes;
+    a.p = p;
+    for (int j = 0; j < nprimes; j++) {
+        if (primes[j] < 2 || primes[j] >= (1ull << 63)) return PMLG_EBADMOD;
+        a.q[j] = primes[j];
+        uint64_t pr = 1 % primes[j];
+        for (int l = 0; l < j; l++) pr = h_mulmod(pr, primes[l] % primes[j], primes[j]);
+        a.ginv[j] = (j == 0) ? 1 : h_invmod(pr, primes[j]);
+        if (j > 0 && a.ginv[j] == 0) {
+            set_error(ctx, "CRT primes are not pairwise coprime");
+            return PMLG_EBADMOD;
+        }
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    prof_begin(ctx, "multimod_crt", st);
+    multimod_crt_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, a);
+    prof_end(ctx, st);
+    count_launch(ctx);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+}  // extern "C"

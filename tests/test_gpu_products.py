@@ -1,0 +1,231 @@
+"""GPU parity tests of the products (through the C ABI, via pml_gb300):
+batched matrix products, nmod_poly_mat_multiply, nmod_poly_mat_mulmid, the
+batched uneven products.  Bit-exact against the oracle and the golden
+fixtures, for both pointwise forms (CUDA-core and INT8 tensor core)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import P998, as_u64, golden, pm_from_seed, to_dev, to_host, vec_from_seed
+
+pytestmark = pytest.mark.gpu
+
+FORMS = [1, 2]   # PMLG_FORM_CUDA_CORE, PMLG_FORM_INT8_TC
+
+
+def _torch():
+    import torch
+    return torch
+
+
+@pytest.fixture(params=FORMS, ids=["cuda_core", "int8_tc"])
+def fctx(request, ctx):
+    ctx.set_form(request.param)
+    yield ctx
+    ctx.set_form(0)
+
+
+# ---------------------------------------------------------------------------
+# batched matrix products (pointwise contraction)
+# ---------------------------------------------------------------------------
+
+def _batch(fctx, A, B, p):
+    import pml_gb300
+    torch = _torch()
+    dA = torch.from_numpy(A.astype(np.uint32).view(np.int32)).cuda()
+    dB = torch.from_numpy(B.astype(np.uint32).view(np.int32)).cuda()
+    C = pml_gb300.nmod_mat_mul_batch(dA, dB, p, ctx=fctx)
+    torch.cuda.synchronize()
+    return C.cpu().numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("case", golden("matmuls"), ids=lambda c: f"p{c['p']}-{c['r']}-s{c['seedA']}")
+def test_batch_matmul_golden(fctx, case):
+    p, r, k, c = case["p"], case["r"], case["k"], case["c"]
+    A = vec_from_seed(r * k, p, case["seedA"]).reshape(1, r, k)
+    B = vec_from_seed(k * c, p, case["seedB"]).reshape(1, k, c)
+    if case["seedA"] == -1:
+        B = A
+    C = _batch(fctx, A, B, p)
+    assert np.array_equal(C[0].astype(np.uint64), as_u64(case["C"]))
+
+
+@pytest.mark.parametrize("shape", [(3, 1, 1, 1), (5, 7, 9, 3), (33, 64, 64, 64), (4, 65, 70, 130), (2, 128, 1, 128)])
+@pytest.mark.parametrize("p", [P998, 7, 536870923, 1073741789])
+def test_batch_matmul_random(fctx, shape, p):
+    nb, r, k, c = shape
+    A = oracle.rand_vec_u32(nb * r * k, p, 1).reshape(nb, r, k)
+    B = oracle.rand_vec_u32(nb * k * c, p, 2).reshape(nb, k, c)
+    C = _batch(fctx, A, B, p)
+    assert np.array_equal(C, oracle.nmod_mat_mul_batch_u32(A, B, p, nthreads=8))
+
+
+def test_batch_matmul_full_size_worst_case(ctx):
+    """4096 x (64x64 . 64x64) mod 998244353: both forms agree with each other
+    and with the oracle on a sample of batches; all-(p-1) batch included."""
+    p = P998
+    nb = 4096
+    A = oracle.rand_vec_u32(nb * 64 * 64, p, 11).reshape(nb, 64, 64)
+    B = oracle.rand_vec_u32(nb * 64 * 64, p, 12).reshape(nb, 64, 64)
+    A[0] = p - 1
+    B[0] = p - 1
+    ctx.set_form(1)
+    C1 = _batch(ctx, A, B, p)
+    ctx.set_form(2)
+    C2 = _batch(ctx, A, B, p)
+    ctx.set_form(0)
+    assert np.array_equal(C1, C2)
+    idx = [0, 1, 1234, 4095]
+    assert np.array_equal(C1[idx], oracle.nmod_mat_mul_batch_u32(A[idx], B[idx], p))
+
+
+# ---------------------------------------------------------------------------
+# nmod_poly_mat_multiply
+# ---------------------------------------------------------------------------
+
+def _mul(fctx, A, B, p):
+    import pml_gb300
+    torch = _torch()
+    C = pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), p, ctx=fctx)
+    torch.cuda.synchronize()
+    return to_host(C)
+
+
+@pytest.mark.parametrize("case", golden("products"), ids=lambda c: f"p{c['p']}-{c['r']}x{c['k']}x{c['c']}-{c['len1']}-{c['len2']}-s{c['seedA']}")
+def test_products_golden(fctx, case):
+    p = case["p"]
+    A = pm_from_seed(case["r"], case["k"], case["len1"], p, case["seedA"])
+    B = pm_from_seed(case["k"], case["c"], case["len2"], p, case["seedB"])
+    assert np.array_equal(_mul(fctx, A, B, p), as_u64(case["C"]))
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1, 1, 1), (2, 3, 4, 17, 33), (7, 5, 3, 64, 1), (9, 70, 3, 40, 25),
+                                  (65, 3, 66, 5, 8), (4, 4, 4, 1000, 1100)])
+@pytest.mark.parametrize("p", [P998, 2, 1000003, 2305843009213693951, 18446744073709551557])
+def test_products_random(fctx, dims, p):
+    r, k, c, l1, l2 = dims
+    A = oracle.rand_poly_mat(r, k, l1, p, 3)
+    B = oracle.rand_poly_mat(k, c, l2, p, 4)
+    assert np.array_equal(_mul(fctx, A, B, p), oracle.poly_mat_mul(A, B, p, nthreads=8))
+
+
+def test_products_config1_plain(fctx):
+    """16x16 . 16x16, degree < 256, p = 998244353 (the CPU-runnable case)."""
+    p = P998
+    A = oracle.rand_poly_mat(16, 16, 256, p, 101)
+    B = oracle.rand_poly_mat(16, 16, 256, p, 102)
+    C = _mul(fctx, A, B, p)
+    assert np.array_equal(C, oracle.poly_mat_mul(A, B, p, nthreads=8))
+
+
+def test_products_empty_and_host_path(ctx):
+    import pml_gb300
+    p = P998
+    # empty inner dimension / zero lengths
+    A = np.zeros((3, 0, 4), dtype=np.uint64)
+    B = np.zeros((0, 2, 5), dtype=np.uint64)
+    C = pml_gb300.nmod_poly_mat_multiply(A, B, p, ctx=ctx)
+    assert C.shape == (3, 2, 8) and not C.any()
+    # host-buffer entry point equals the device one
+    A = oracle.rand_poly_mat(5, 6, 40, p, 7)
+    B = oracle.rand_poly_mat(6, 4, 30, p, 8)
+    Ch = pml_gb300.nmod_poly_mat_multiply(A, B, p, ctx=ctx)
+    assert np.array_equal(Ch, oracle.poly_mat_mul(A, B, p))
+
+
+def test_products_alias_rejected(ctx):
+    """An output overlapping an input is refused (PMLG_EALIAS), nothing runs."""
+    torch = _torch()
+    p = P998
+    buf = to_dev(oracle.rand_poly_mat(2, 2, 16, p, 1))
+    ptr = buf.data_ptr()
+    st = torch.cuda.current_stream().cuda_stream
+    status = ctx.lib.pmlg_poly_mat_mul(ctx.handle, ptr, ptr, ptr, 2, 2, 2, 4, 4, p, st)
+    assert status == 5
+    torch.cuda.synchronize()
+
+
+def test_products_full_size_property(ctx):
+    """64x64 . 64x64, degree < 4096: C(a) = A(a) B(a) mod p at random points a
+    (size-independent check, Schwartz-Zippel), both forms bit-identical."""
+    torch = _torch()
+    import pml_gb300
+    p = P998
+    A = oracle.rand_poly_mat(64, 64, 4096, p, 21)
+    B = oracle.rand_poly_mat(64, 64, 4096, p, 22)
+    dA, dB = to_dev(A), to_dev(B)
+    ctx.set_form(1)
+    C1 = to_host(pml_gb300.nmod_poly_mat_multiply(dA, dB, p, ctx=ctx))
+    ctx.set_form(2)
+    C2 = to_host(pml_gb300.nmod_poly_mat_multiply(dA, dB, p, ctx=ctx))
+    ctx.set_form(0)
+    torch.cuda.synchronize()
+    assert np.array_equal(C1, C2)
+    rng = np.random.default_rng(5)
+    for _ in range(2):
+        a = np.uint64(int(rng.integers(1, p)))
+
+        def ev(P):
+            # Horner over the coefficients, vectorised over the entries (values < 2^30)
+            acc = np.zeros(P.shape[:2], dtype=np.uint64)
+            for d in range(P.shape[2] - 1, -1, -1):
+                acc = (acc * a + P[:, :, d]) % np.uint64(p)
+            return acc.astype(object)
+        Ea, Eb, Ec = ev(A), ev(B), ev(C1)
+        assert ((Ea.dot(Eb)) % p == Ec).all()
+
+
+# ---------------------------------------------------------------------------
+# nmod_poly_mat_mulmid
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("case", golden("mulmids"), ids=lambda c: f"p{c['p']}-{c['len1']}-{c['len2']}-{c['nlo']}-{c['nhi']}")
+def test_mulmid_golden(fctx, case):
+    import pml_gb300
+    p = case["p"]
+    A = pm_from_seed(case["r"], case["k"], case["len1"], p, case["seedA"])
+    B = pm_from_seed(case["k"], case["c"], case["len2"], p, case["seedB"])
+    res, n = pml_gb300.nmod_poly_mat_mulmid(to_dev(A), to_dev(B), case["nlo"], case["nhi"], p, ctx=fctx,
+                                            want_length=True)
+    assert n == case["len"]
+    assert np.array_equal(to_host(res), as_u64(case["res"]))
+
+
+@pytest.mark.parametrize("args", [(4, 4, 2, 9, 64, 32, 64), (8, 8, 4, 17, 64, 32, 64), (3, 3, 3, 50, 50, 10, 200),
+                                  (2, 5, 3, 100, 7, 0, 3), (64, 64, 32, 129, 512, 256, 512)])
+@pytest.mark.parametrize("p", [P998, 1000003, 2305843009213693951])
+def test_mulmid_random(fctx, args, p):
+    import pml_gb300
+    r, k, c, l1, l2, nlo, nhi = args
+    A = oracle.rand_poly_mat(r, k, l1, p, 31)
+    B = oracle.rand_poly_mat(k, c, l2, p, 32)
+    res, n = pml_gb300.nmod_poly_mat_mulmid(to_dev(A), to_dev(B), nlo, nhi, p, ctx=fctx, want_length=True)
+    ref, nref = oracle.poly_mat_mulmid(A, B, nlo, nhi, p, nthreads=8)
+    assert n == nref
+    assert np.array_equal(to_host(res), ref)
+
+
+# ---------------------------------------------------------------------------
+# batched uneven products
+# ---------------------------------------------------------------------------
+
+def test_batched_uneven(ctx):
+    """Mixed sizes and moduli (half NTT prime, half 59-bit primes) in one call."""
+    import pml_gb300
+    torch = _torch()
+    rng = np.random.default_rng(9)
+    jobs, refs = [], []
+    for i in range(12):
+        m = int(rng.integers(4, 13))
+        L = int(2 ** rng.uniform(3, 7))
+        p = P998 if i % 2 == 0 else oracle.rand_prime(59, 1000 + i)
+        A = oracle.rand_poly_mat(m, m, L, p, 2 * i)
+        B = oracle.rand_poly_mat(m, m, L, p, 2 * i + 1)
+        jobs.append((to_dev(A), to_dev(B), p))
+        refs.append(oracle.poly_mat_mul(A, B, p))
+    outs = pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx)
+    torch.cuda.synchronize()
+    for o, ref in zip(outs, refs):
+        assert np.array_equal(to_host(o), ref)
