@@ -51,7 +51,37 @@ def parse():
     ap.add_argument("--impl", choices=["pml", "reference"], default="pml")
     ap.add_argument("--no-pmbasis", action="store_true", help="skip the pmbasis measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--profile-case", choices=["product", "pmbasis"], default=None,
+                    help="run one product per form (or one pmbasis at order 1024) and exit: "
+                         "the small case for kernel captures")
     return ap.parse_args()
+
+
+def run_profile_case(args):
+    """One headline product with each form (INT8 first), or one pmbasis 64x32 at
+    order 1024: a short, fixed launch sequence for profiler captures."""
+    import torch
+    import pml_gb300
+    ctx = pml_gb300.Context(0)
+    if args.profile_case == "product":
+        A, B = make_inputs(1)
+        dA = torch.from_numpy(A.view(np.int64)).cuda()
+        dB = torch.from_numpy(B.view(np.int64)).cuda()
+        outs = []
+        for form in (pml_gb300.FORM_INT8_TC, pml_gb300.FORM_CUDA_CORE):
+            ctx.set_form(form)
+            outs.append(pml_gb300.nmod_poly_mat_multiply(dA, dB, P, ctx=ctx))
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "product", "forms_agree": bool(torch.equal(outs[0], outs[1])),
+                          "launches": ctx.launches}))
+    else:
+        rng = np.random.default_rng(7)
+        F = rng.integers(0, P, size=(PM_M, PM_N, 1024), dtype=np.uint64)
+        ab, sh = pml_gb300.nmod_poly_mat_pmbasis(torch.from_numpy(F.view(np.int64)).cuda(), 1024, [0] * PM_M, P,
+                                                 ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "pmbasis", "rdeg_sum": int(sum(sh)), "launches": ctx.launches}))
+    ctx.close()
 
 
 def dist_env():
@@ -390,7 +420,9 @@ def run_pml(args):
 
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_pml(args)

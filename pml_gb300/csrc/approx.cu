@@ -20,6 +20,7 @@
 #include "polymat.cuh"
 #include "ntt.cuh"
 
+#include <cooperative_groups.h>
 #include <vector>
 
 namespace pmlg {
@@ -33,11 +34,12 @@ struct LeafArgs
     int64_t ldF, flen;
     uint64_t *out;
     int64_t ldo;
-    uint32_t *R;      // [order][m][n]
-    uint32_t *AB;     // [order+1][m][m]
+    uint32_t *R;      // [order][m][n]   (general kernel only)
+    uint32_t *AB;     // [order+1][m][m] (general kernel only)
     int64_t *shift;   // device, m entries
     int m, n, order;
     uint32_t p, r32, r32q, oneq;
+    uint32_t pneg;    // -p^{-1} mod 2^32 (Montgomery reduction)
 };
 
 __device__ __forceinline__ uint32_t mulmod32(uint32_t a, uint32_t b, const LeafArgs &A)
@@ -74,7 +76,7 @@ mbasis_leaf_kernel(LeafArgs a)
     __shared__ int pivrow[LEAF_MAX], nprow[LEAF_MAX];
     __shared__ int used[LEAF_MAX];
     __shared__ long long sh[LEAF_MAX];
-    __shared__ int s_pl[2], s_rank, s_nn, s_alen, s_grow, s_stop;
+    __shared__ int s_pl[2], s_rank, s_nn, s_alen, s_grow;
 
     const int tid = threadIdx.x, nth = blockDim.x;
     const int m = a.m, n = a.n, order = a.order;
@@ -88,7 +90,7 @@ mbasis_leaf_kernel(LeafArgs a)
     for (int64_t idx = tid; idx < (int64_t)(order + 1) * m * m; idx += nth)
         a.AB[idx] = (idx < m * m && (idx / m) == (idx % m)) ? 1u : 0u;
     if (tid < m) sh[tid] = a.shift[tid];
-    if (tid == 0) { s_alen = 1; s_stop = 0; }
+    if (tid == 0) s_alen = 1;
     __syncthreads();
 
     for (int ord = 0; ord < order; ord++) {
@@ -261,6 +263,279 @@ mbasis_leaf_kernel(LeafArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// cluster leaf: m <= 64, n <= 32, order <= 32
+// ---------------------------------------------------------------------------
+//
+// One leaf runs on a cluster of LC_CL CTAs (one per SM).  CTA c keeps, in its
+// own shared memory, the columns [c*cm, (c+1)*cm) of every coefficient of
+// appbas and the columns [c*cn, (c+1)*cn) of every coefficient of the
+// residual R.  Each step:
+//   1. every CTA computes the same stable shift permutation;
+//   2. every CTA writes its slice of the permuted R[ord] (transposed) into
+//      CTA 0's shared memory (distributed shared memory stores); cluster barrier;
+//   3. CTA 0 runs the elimination with 4 warps: lane j holds row j of
+//      E = R[ord]^T (j < n <= 32), warp w holds columns [16w, 16w+16) in
+//      registers; column c's owner warp finds the pivot with a ballot and
+//      publishes it through shared memory (double-buffered, one named barrier
+//      per column); every warp updates its columns with pivot row values taken
+//      by warp shuffles.  Updates are division-free,
+//      row_j <- (pv * row_j - f_j * row_pl) * 2^-32 mod p (Montgomery
+//      reduction): every row operation only scales rows, so the ratios
+//      E[pl_b][np_a] / E[pl_b][pc_b] at the end are the RREF entries;
+//   4. CTA 0 computes X and writes X, the pivot rows and the rank into every
+//      CTA; cluster barrier;
+//   5. every CTA updates its slices (non-pivot rows += X * pivot rows, pivot
+//      rows times x) and the shift.
+// appbas' length is tracked as an upper bound (+1 per step); the output is
+// zero beyond the actual length, which the host reads back.
+
+constexpr int LC_CL = 8;
+constexpr int LC_THREADS = 512;
+constexpr int LC_MAXM = 64, LC_MAXN = 32, LC_MAXORD = 32;
+
+__device__ __forceinline__ uint32_t redc(uint64_t t, uint32_t p, uint32_t pneg)
+{
+    // t < p * 2^31: returns t * 2^-32 mod p in [0, p)
+    const uint32_t mq = (uint32_t)t * pneg;
+    const uint64_t u = t + (uint64_t)mq * p;
+    const uint32_t r = (uint32_t)(u >> 32);
+    return r >= p ? r - p : r;
+}
+
+__device__ __forceinline__ void bar_elim() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+struct LcShared
+{
+    uint32_t E[LC_MAXN][LC_MAXM + 1];   // gathered R[ord]^T (CTA 0)
+    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank (every CTA)
+    int pivrow[LC_MAXM], nprow[LC_MAXM];
+    int info[2];                        // rank, nullity
+    long long sh[LC_MAXM];
+    int perm[LC_MAXM];
+    uint32_t fbuf[2][32];
+    uint32_t pvbuf[2];
+    int plbuf[2];
+    int pivlane[LC_MAXM], pivcol[LC_MAXM], nonpiv[LC_MAXM];
+    uint32_t inv[LC_MAXM];
+};
+
+__global__ void __cluster_dims__(LC_CL, 1, 1) __launch_bounds__(LC_THREADS)
+mbasis_leaf_cluster_kernel(LeafArgs a)
+{
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    __shared__ LcShared S;
+    extern __shared__ uint32_t dyn[];
+    const int c = (int)cluster.block_rank();
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int m = a.m, n = a.n, order = a.order;
+    const uint32_t p = a.p;
+    const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
+    const int m0 = c * ncm, n0 = c * ncn;
+    const int cm = m0 < m ? (m - m0 < ncm ? m - m0 : ncm) : 0;
+    const int cn = n0 < n ? (n - n0 < ncn ? n - n0 : ncn) : 0;
+    uint32_t *AB = dyn;                                      // [order+1][m][ncm]
+    uint32_t *R = dyn + (size_t)(order + 1) * m * ncm;       // [order][m][ncn]
+    const int64_t fl = a.flen < order ? a.flen : order;
+
+    for (int idx = tid; idx < order * m * ncn; idx += nth) {
+        const int d = idx / (m * ncn), rem = idx - d * m * ncn, i = rem / ncn, jl = rem - i * ncn;
+        uint32_t v = 0;
+        if (jl < cn && d < fl) v = (uint32_t)a.F[((int64_t)i * n + n0 + jl) * a.ldF + d];
+        R[idx] = v;
+    }
+    for (int idx = tid; idx < (order + 1) * m * ncm; idx += nth) {
+        const int d = idx / (m * ncm), rem = idx - d * m * ncm, i = rem / ncm, il = rem - i * ncm;
+        AB[idx] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
+    }
+    if (tid < m) S.sh[tid] = a.shift[tid];
+    int alen = 1;
+    uint32_t *E0 = cluster.map_shared_rank(&S.E[0][0], 0);
+    cluster.sync();
+
+    for (int ord = 0; ord < order; ord++) {
+        // 1. stable shift permutation (identical in every CTA)
+        if (tid < m) {
+            int r = 0;
+            const long long v = S.sh[tid];
+            for (int i = 0; i < m; i++) r += (S.sh[i] < v) || (S.sh[i] == v && i < tid);
+            S.perm[r] = tid;
+        }
+        __syncthreads();
+        // 2. gather the permuted R[ord]^T into CTA 0
+        for (int idx = tid; idx < m * cn; idx += nth) {
+            const int r = idx / cn, jl = idx - r * cn;
+            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[((size_t)ord * m + S.perm[r]) * ncn + jl];
+        }
+        cluster.sync();
+
+        // 3. elimination in CTA 0
+        if (c == 0 && tid < 128) {
+            const int w = tid >> 5, lane = tid & 31;
+            uint32_t x[16];
+#pragma unroll
+            for (int k = 0; k < 16; k++) x[k] = (lane < n && 16 * w + k < m) ? S.E[lane][16 * w + k] : 0u;
+            unsigned used = 0;
+            int rank = 0, nn = 0;
+            for (int cw = 0; cw < 4; cw++) {
+#pragma unroll
+                for (int cl = 0; cl < 16; cl++) {
+                    const int col = cw * 16 + cl;
+                    if (col >= m) break;
+                    const int buf = col & 1;
+                    if (w == cw) {
+                        const uint32_t v = x[cl];
+                        const unsigned cand =
+                            __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
+                        const int pl = cand ? __ffs(cand) - 1 : -1;
+                        S.fbuf[buf][lane] = v;
+                        if (lane == 0) S.plbuf[buf] = pl;
+                        if (lane == pl) S.pvbuf[buf] = v;
+                    }
+                    bar_elim();
+                    const int pl = S.plbuf[buf];
+                    if (pl < 0) {
+                        if (tid == 0) S.nonpiv[nn] = col;
+                        nn++;
+                        continue;
+                    }
+                    const uint32_t pv = S.pvbuf[buf];
+                    const uint32_t f = S.fbuf[buf][lane];
+                    const uint32_t nf = f ? p - f : 0u;
+#pragma unroll
+                    for (int k = 0; k < 16; k++) {
+                        const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
+                        if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
+                    }
+                    used |= 1u << pl;
+                    if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
+                    rank++;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 16; k++)
+                if (lane < n && 16 * w + k < m) S.E[lane][16 * w + k] = x[k];
+            if (tid == 0) { S.info[0] = rank; S.info[1] = m - rank; }
+        }
+        __syncthreads();
+        if (c == 0) {
+            const int rank = S.info[0], nullity = S.info[1];
+            if (rank > 0 && nullity > 0) {
+                if (tid < rank) {
+                    // Fermat inverse of the pivot value
+                    uint32_t b = S.E[S.pivlane[tid]][S.pivcol[tid]], r = 1;
+                    for (uint32_t e = p - 2; e; e >>= 1) {
+                        if (e & 1) r = mod64_q((uint64_t)r * b, p, a.r32, a.r32q, a.oneq);
+                        b = mod64_q((uint64_t)b * b, p, a.r32, a.r32q, a.oneq);
+                    }
+                    S.inv[tid] = r;
+                }
+                __syncthreads();
+                // X and the row indices, written into every CTA of the cluster
+                for (int idx = tid; idx < nullity * rank; idx += nth) {
+                    const int ia = idx / rank, b = idx - ia * rank;
+                    const uint32_t v = mod64_q((uint64_t)S.E[S.pivlane[b]][S.nonpiv[ia]] * S.inv[b], p,
+                                               a.r32, a.r32q, a.oneq);
+                    const uint32_t xv = v ? p - v : 0u;
+                    for (int cc = 0; cc < LC_CL; cc++) cluster.map_shared_rank(&S.X[0][0], cc)[ia * LC_MAXM + b] = xv;
+                }
+                for (int idx = tid; idx < LC_CL * m; idx += nth) {
+                    const int cc = idx / m, i = idx - cc * m;
+                    if (i < rank) cluster.map_shared_rank(S.pivrow, cc)[i] = S.perm[S.pivcol[i]];
+                    else cluster.map_shared_rank(S.nprow, cc)[i - rank] = S.perm[S.nonpiv[i - rank]];
+                }
+            }
+            if (tid < LC_CL) {
+                cluster.map_shared_rank(S.info, tid)[0] = rank;
+                cluster.map_shared_rank(S.info, tid)[1] = nullity;
+            }
+        }
+        cluster.sync();
+
+        const int rank = S.info[0], nullity = S.info[1];
+        if (nullity == 0) {
+            // appbas = x^(order-ord) * appbas, shift += order - ord
+            const int k = order - ord;
+            for (int idx = tid; idx < m * ncm; idx += nth) {
+                for (int d = alen - 1; d >= 0; d--) AB[((size_t)(d + k)) * m * ncm + idx] = AB[(size_t)d * m * ncm + idx];
+                for (int d = 0; d < k; d++) AB[(size_t)d * m * ncm + idx] = 0;
+            }
+            if (tid < m) S.sh[tid] += k;
+            alen += k;
+            __syncthreads();
+            break;
+        }
+        if (rank == 0) continue;
+
+        // 5a. non-pivot rows += X * pivot rows (appbas d < alen, R ord < d < order)
+        const int nab = nullity * alen * cm;
+        const int nr = nullity * (order - ord - 1) * cn;
+        for (int idx = tid; idx < nab + nr; idx += nth) {
+            uint32_t *base;
+            int row, width, col, ia;
+            if (idx < nab) {
+                ia = idx / (alen * cm);
+                const int rem = idx - ia * alen * cm, d = rem / cm;
+                col = rem - d * cm;
+                width = ncm;
+                base = AB + (size_t)d * m * ncm;
+            } else {
+                const int j2 = idx - nab;
+                ia = j2 / ((order - ord - 1) * cn);
+                const int rem = j2 - ia * (order - ord - 1) * cn, d = ord + 1 + rem / cn;
+                col = rem % cn;
+                width = ncn;
+                base = R + (size_t)d * m * ncn;
+            }
+            row = S.nprow[ia];
+            uint64_t acc = base[row * width + col];
+            int b = 0;
+            for (; b + 8 <= rank; b += 8) {
+#pragma unroll
+                for (int u = 0; u < 8; u++) acc += (uint64_t)S.X[ia][b + u] * base[S.pivrow[b + u] * width + col];
+                acc = fold(acc, a.r32);
+            }
+            for (; b < rank; b++) acc += (uint64_t)S.X[ia][b] * base[S.pivrow[b] * width + col];
+            base[row * width + col] = mod64_q(acc, p, a.r32, a.r32q, a.oneq);
+        }
+        __syncthreads();
+        // 5b. pivot rows times x; length bound grows by one
+        const int nlen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
+        for (int idx = tid; idx < rank * (cm + cn); idx += nth) {
+            const int b = idx / (cm + cn), col = idx - b * (cm + cn);
+            const int row = S.pivrow[b];
+            if (col < cm) {
+                for (int d = nlen - 1; d > 0; d--)
+                    AB[(size_t)d * m * ncm + row * ncm + col] = AB[(size_t)(d - 1) * m * ncm + row * ncm + col];
+                AB[row * ncm + col] = 0;
+            } else {
+                const int j = col - cm;
+                for (int d = order - 1; d > ord; d--)
+                    R[(size_t)d * m * ncn + row * ncn + j] = R[(size_t)(d - 1) * m * ncn + row * ncn + j];
+            }
+        }
+        if (tid < rank) S.sh[S.pivrow[tid]] += 1;
+        alen = nlen;
+        __syncthreads();
+    }
+
+    // output: columns of this CTA, entry-major, zero beyond the length bound
+    for (int64_t idx = tid; idx < (int64_t)m * cm * a.ldo; idx += nth) {
+        const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
+        const int i = (int)(e / cm), il = (int)(e - (int64_t)i * cm);
+        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < alen ? (uint64_t)AB[(size_t)d * m * ncm + i * ncm + il] : 0ull;
+    }
+    if (c == 0 && tid < m) a.shift[tid] = S.sh[tid];
+    cluster.sync();   // no CTA leaves while another may still address its shared memory
+}
+
+static size_t leaf_cluster_smem(int m, int n, int order)
+{
+    const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
+    return ((size_t)(order + 1) * m * ncm + (size_t)order * m * ncn) * sizeof(uint32_t);
+}
+
+// ---------------------------------------------------------------------------
 // host recursion
 // ---------------------------------------------------------------------------
 
@@ -316,11 +591,30 @@ static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, i
     a.r32 = (uint32_t)((1ull << 32) % S.p);
     a.r32q = h_shoup_q(a.r32, a.p);
     a.oneq = (uint32_t)((1ull << 32) / S.p);
-    prof_begin(S.ctx, "mbasis_leaf", S.st);
-    mbasis_leaf_kernel<<<1, LEAF_THREADS, 0, S.st>>>(a);
-    prof_end(S.ctx, S.st);
-    count_launch(S.ctx);
+    {
+        uint32_t inv = a.p;                       // Newton iteration for p^{-1} mod 2^32 (p odd)
+        for (int i = 0; i < 5; i++) inv *= 2u - a.p * inv;
+        a.pneg = 0u - inv;
+    }
     pmlg_ctx *ctx = S.ctx;
+    const bool cluster = (a.p & 1u) && S.m <= LC_MAXM && S.n <= LC_MAXN && order <= LC_MAXORD;
+    if (cluster) {
+        const size_t smem = leaf_cluster_smem(a.m, a.n, a.order);
+        static size_t attr = 0;
+        if (smem > attr) {
+            PMLG_CUDA_TRY(cudaFuncSetAttribute(mbasis_leaf_cluster_kernel,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr = smem;
+        }
+        prof_begin(ctx, "mbasis_leaf_cluster", S.st);
+        mbasis_leaf_cluster_kernel<<<LC_CL, LC_THREADS, smem, S.st>>>(a);
+        prof_end(ctx, S.st);
+    } else {
+        prof_begin(ctx, "mbasis_leaf", S.st);
+        mbasis_leaf_kernel<<<1, LEAF_THREADS, 0, S.st>>>(a);
+        prof_end(ctx, S.st);
+    }
+    count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
     S.ar.top = mark;
     return PMLG_OK;

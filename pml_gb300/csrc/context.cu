@@ -178,6 +178,7 @@ int make_plan(pmlg_ctx *ctx, uint64_t p, int lg, int64_t inner, int64_t minlen, 
         return PMLG_EBADMOD;
     }
     if (p < (1ull << 30) && ((p - 1) >> lg) << lg == p - 1 && h_is_prime(p)) {
+        plan->direct = 1;
         plan->t = 1;
         plan->q[0] = (uint32_t)p;
         plan->qp[0] = 0;
@@ -208,6 +209,7 @@ int make_plan(pmlg_ctx *ctx, uint64_t p, int lg, int64_t inner, int64_t minlen, 
         set_error(ctx, "modulus too large for %d CRT primes", kMaxPrimes);
         return PMLG_EBADMOD;
     }
+    plan->direct = 0;
     plan->t = t;
     for (int j = 0; j < t; j++) plan->q[j] = kCrtPrimes[j];
     for (int j = 0; j < t; j++) {

@@ -240,12 +240,12 @@ ntt_inv_kernel(NttInvArgs a)
         if (d < 0 || d >= a.cnt) continue;
         uint32_t val = shoup_mul(v[m], T.ninv, T.ninvq, T.q);
         val = val >= T.q ? val - T.q : val;
-        if (a.t == 1)
+        if (a.direct)
             a.out64[e * a.out_ld + d] = val;
         else
             a.res32[(j * a.nent + e) * a.cnt + d] = val;
     }
-    if (a.t == 1)
+    if (a.direct)
         for (int64_t d = a.cnt + t; d < a.out_cap; d += TPT) a.out64[e * a.out_ld + d] = 0;
 }
 

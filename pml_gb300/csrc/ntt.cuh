@@ -39,12 +39,12 @@ struct NttInvArgs
     int64_t prime_stride, tile_stride;
     int64_t nent;
     int64_t lo, cnt;        // coefficients [lo, lo + cnt) of the length-N cyclic result
-    // direct output (t == 1): out64[e * out_ld + d], d < out_cap, zero for d >= cnt
+    // direct output (p is the NTT prime): out64[e * out_ld + d], d < out_cap, zero for d >= cnt
     uint64_t *out64;
     int64_t out_ld, out_cap;
-    // CRT output (t > 1): res32[(j * nent + e) * cnt + d]
+    // CRT output (otherwise): res32[(j * nent + e) * cnt + d]
     uint32_t *res32;
-    int lg, t;
+    int lg, t, direct;
     NttDev tab[kMaxPrimes];
 };
 

@@ -79,7 +79,8 @@ constexpr int kMaxPrimes = 6;
 
 struct CrtPlan
 {
-    int t;                         // number of primes (1 = direct, no CRT)
+    int direct;                    // 1: p itself is the (single) NTT prime, no CRT
+    int t;                         // number of primes
     uint32_t q[kMaxPrimes];
     // garner[j][l] = q_l mod q_j (l < j), ginv[j] = (q_0..q_{j-1})^{-1} mod q_j
     uint32_t qmod[kMaxPrimes][kMaxPrimes];

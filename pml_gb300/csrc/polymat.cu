@@ -32,7 +32,7 @@ size_t product_scratch_bytes(const ProductJob &j, const CrtPlan &plan)
     b += align256(t * N * j.r * j.k * 4);
     b += align256(t * N * j.k * j.c * 4);
     b += align256(t * N * j.r * j.c * 4);
-    if (t > 1) b += align256(t * j.r * j.c * j.cnt * 4);
+    if (!plan.direct) b += align256(t * j.r * j.c * j.cnt * 4);
     return b;
 }
 
@@ -46,7 +46,7 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
     uint32_t *EA = (uint32_t *)w; w += align256((size_t)t * N * nA * 4);
     uint32_t *EB = (uint32_t *)w; w += align256((size_t)t * N * nB * 4);
     uint32_t *EC = (uint32_t *)w; w += align256((size_t)t * N * nC * 4);
-    uint32_t *R32 = (t > 1) ? (uint32_t *)w : nullptr;
+    uint32_t *R32 = plan.direct ? nullptr : (uint32_t *)w;
 
     const NttTable *tabs[kMaxPrimes];
     for (int i = 0; i < t; i++) PMLG_TRY(get_table(ctx, plan.q[i], j.lg, &tabs[i]));
@@ -54,7 +54,7 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
     NttFwdArgs fa{};
     fa.lg = j.lg;
     fa.t = t;
-    fa.reduce = (t > 1);
+    fa.reduce = !plan.direct;
     for (int i = 0; i < t; i++)
         fa.tab[i] = NttDev{tabs[i]->d_w, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
                            tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
@@ -89,12 +89,12 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
     ia.lo = j.lo; ia.cnt = j.cnt;
     ia.out64 = j.C; ia.out_ld = j.ldc; ia.out_cap = j.c_cap;
     ia.res32 = R32;
-    ia.lg = j.lg; ia.t = t;
+    ia.lg = j.lg; ia.t = t; ia.direct = plan.direct;
     for (int i = 0; i < t; i++)
         ia.tab[i] = NttDev{tabs[i]->d_iw, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
                            tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
     PMLG_TRY(ntt_inverse(ctx, ia, st));
-    if (t > 1) PMLG_TRY(crt_combine(ctx, plan, R32, nC, j.cnt, j.C, j.ldc, j.c_cap, st));
+    if (!plan.direct) PMLG_TRY(crt_combine(ctx, plan, R32, nC, j.cnt, j.C, j.ldc, j.c_cap, st));
     return PMLG_OK;
 }
 
