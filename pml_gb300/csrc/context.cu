@@ -110,20 +110,22 @@ int get_table(pmlg_ctx *ctx, uint32_t q, int lg, const NttTable **out)
     const uint64_t iwN = h_invmod(wN, q);
     uint32_t *hw = (uint32_t *)malloc(4 * N * sizeof(uint32_t));
     if (!hw) return PMLG_ENOMEM;
-    // interleaved {w, w'} pairs: forward table in [0, 2N), inverse in [2N, 4N)
+    // interleaved {w^e, quotient} pairs: forward powers in [0, 2N), inverse in [2N, 4N)
     uint32_t *hf = hw, *hi = hw + 2 * N;
-    hf[0] = hi[0] = 1;
-    hf[1] = hi[1] = h_shoup_q(1, q);
-    for (uint64_t h = 1; h < N; h <<= 1) {
-        const uint64_t wh = h_powmod(wN, N / (2 * h), q);
-        const uint64_t iwh = h_powmod(iwN, N / (2 * h), q);
+    {
         uint64_t x = 1, y = 1;
-        for (uint64_t j = 0; j < h; j++) {
-            hf[2 * (h + j)] = (uint32_t)x; hf[2 * (h + j) + 1] = h_shoup_q((uint32_t)x, q);
-            hi[2 * (h + j)] = (uint32_t)y; hi[2 * (h + j) + 1] = h_shoup_q((uint32_t)y, q);
-            x = h_mulmod(x, wh, q);
-            y = h_mulmod(y, iwh, q);
+        for (uint64_t j = 0; j < N; j++) {
+            hf[2 * j] = (uint32_t)x; hf[2 * j + 1] = h_shoup_q((uint32_t)x, q);
+            hi[2 * j] = (uint32_t)y; hi[2 * j + 1] = h_shoup_q((uint32_t)y, q);
+            x = h_mulmod(x, wN, q);
+            y = h_mulmod(y, iwN, q);
         }
+    }
+    // consistency: w^N = 1 and w^(N/2) = -1, so w is a primitive N-th root
+    if (h_mulmod(hf[2 * (N - 1)], wN, q) != 1 || hf[2 * (N / 2)] != q - 1) {
+        free(hw);
+        set_error(ctx, "root of unity check failed");
+        return PMLG_EINVAL;
     }
     // exact check of every Shoup quotient: w' * q <= w * 2^32 < (w' + 1) * q
     for (uint64_t i = 0; i < 2 * N; i++) {
@@ -154,6 +156,13 @@ int get_table(pmlg_ctx *ctx, uint32_t q, int lg, const NttTable **out)
     }
     T.d_w = (uint2 *)d;
     T.d_iw = T.d_w + N;
+    for (int j = 0; j < 8; j++) {
+        const uint64_t ex = (uint64_t)j * (N / 16);
+        T.c16[j] = (uint32_t)h_powmod(wN, ex, q);
+        T.c16q[j] = h_shoup_q(T.c16[j], q);
+        T.ic16[j] = (uint32_t)h_powmod(iwN, ex, q);
+        T.ic16q[j] = h_shoup_q(T.ic16[j], q);
+    }
     T.ninv = (uint32_t)h_invmod(N % q, q);
     T.ninvq = h_shoup_q(T.ninv, q);
     T.r32 = (uint32_t)((1ull << 32) % q);

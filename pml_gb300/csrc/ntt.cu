@@ -1,13 +1,18 @@
 // ntt.cu -- shared-memory NTT kernels (one transform per 1/tpc of a CTA).
 //
 // Each thread owns 16 residues.  The log2(N) radix-2 stages are processed in
-// groups of up to four stages: inside a group, every thread runs a radix-16
-// (or smaller) sub-transform entirely in registers, with the twiddles of the
-// full transform; between groups the residues go through shared memory once
-// (padded by one word every 16 to avoid bank conflicts).  Forward transforms
-// are decimation in frequency (natural order in, bit-reversed out), inverse
-// ones decimation in time (bit-reversed in, natural out), so no reordering
-// pass is needed.  Butterflies are lazy: values stay below 4q < 2^32.
+// groups of four (the last forward / first inverse group may be shorter):
+// inside a group every thread runs a radix-16 sub-transform in registers.
+// Its butterflies only need the constant sixteenth roots of unity; the part of
+// the twiddles that depends on the sub-transform's offset factors out of every
+// butterfly of the group (it is common to each difference branch) and is
+// applied once per residue, after the group for decimation in frequency and
+// before it for decimation in time: slot m gets w_span^(off * bitrev4(m)).
+// Between groups the residues go through shared memory (padded by one word
+// every 16 against bank conflicts).  Forward transforms are decimation in
+// frequency (natural order in, bit-reversed out), inverse ones decimation in
+// time (bit-reversed in, natural out): no reordering pass.  Values stay in
+// [0, 2q) between butterflies (q < 2^30, lazy reduction).
 #include "ntt.cuh"
 
 namespace pmlg {
@@ -15,7 +20,7 @@ namespace pmlg {
 __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 
 // Index of register slot (u, m) for a thread t in a group whose sub-transforms
-// have 2^G elements spaced `lowstride` (= 2^lls) apart inside blocks of `span`.
+// have 2^G elements spaced 2^lls apart inside blocks of `span`.
 __device__ __forceinline__ int grp_index(int t, int u, int m, int G, int lls, int span)
 {
     const int sub = 16 >> G;
@@ -25,103 +30,82 @@ __device__ __forceinline__ int grp_index(int t, int u, int m, int G, int lls, in
     return blk * span + off + (m << lls);
 }
 
-// DIF stages h = H, H/2, ..., H >> (G-1) on the registers of one thread.
+__device__ __forceinline__ uint32_t csub(uint32_t x, uint32_t m) { return min(x, x - m); }
+
+// Radix-2^G decimation-in-frequency butterflies on each of the 16 >> G
+// sub-transforms held by a thread, with the constant twiddles
+// w_{2^(G-l)}^(m mod half) = c16[(m mod half) * 16 / 2^(G-l)] of stage l.
 template <int G>
-__device__ __forceinline__ void dif_group(uint32_t (&v)[16], int t, int H, const uint2 *__restrict__ w,
-                                          uint32_t q)
+__device__ __forceinline__ void dif_const(uint32_t (&v)[16], const NttDev &T)
 {
-    const uint32_t q2 = 2 * q;
-    const int lowstride = H >> (G - 1);
-    constexpr int SUB = 16 >> G;
-    constexpr int M = 1 << G;
+    constexpr int M = 1 << G, SUB = 16 >> G;
+    const uint32_t q = T.q, q2 = 2 * q;
 #pragma unroll
-    for (int u = 0; u < SUB; u++) {
-        const int sp = t * SUB + u;
-        const int off = sp & (lowstride - 1);
+    for (int u = 0; u < SUB; u++)
 #pragma unroll
         for (int l = 0; l < G; l++) {
-            const int h = H >> l;
             const int half = M >> (l + 1);
 #pragma unroll
             for (int m = 0; m < M; m++) {
                 if (m & half) continue;
-                const int jj = (off + m * lowstride) & (h - 1);
-                const uint2 tw = __ldg(&w[h + jj]);
+                const int ti = (m % half) * (16 >> (G - l));
                 const uint32_t a = v[u * M + m], b = v[u * M + m + half];
-                uint32_t s = a + b;
-                s = s >= q2 ? s - q2 : s;
-                v[u * M + m] = s;
-                v[u * M + m + half] = shoup_mul(a + q2 - b, tw.x, tw.y, q);
+                v[u * M + m] = csub(a + b, q2);
+                const uint32_t d = a + q2 - b;
+                v[u * M + m + half] = ti ? shoup_mul(d, T.c16[ti], T.c16q[ti], q) : csub(d, q2);
             }
         }
-    }
 }
 
-// DIT stages h = Hlow, 2 Hlow, ..., Hlow << (G-1) on the registers of one thread.
+// Radix-2^G decimation-in-time butterflies, constant twiddles
+// w_{2^(l+1)}^-(m mod 2^l) = c16[(m mod 2^l) * 16 / 2^(l+1)] (inverse table).
 template <int G>
-__device__ __forceinline__ void dit_group(uint32_t (&v)[16], int t, int Hlow, const uint2 *__restrict__ w,
-                                          uint32_t q)
+__device__ __forceinline__ void dit_const(uint32_t (&v)[16], const NttDev &T)
 {
-    const uint32_t q2 = 2 * q;
-    constexpr int SUB = 16 >> G;
-    constexpr int M = 1 << G;
+    constexpr int M = 1 << G, SUB = 16 >> G;
+    const uint32_t q = T.q, q2 = 2 * q;
 #pragma unroll
-    for (int u = 0; u < SUB; u++) {
-        const int sp = t * SUB + u;
-        const int off = sp & (Hlow - 1);
+    for (int u = 0; u < SUB; u++)
 #pragma unroll
         for (int l = 0; l < G; l++) {
-            const int h = Hlow << l;
             const int half = 1 << l;
 #pragma unroll
             for (int m = 0; m < M; m++) {
                 if (m & half) continue;
-                const int jj = (off + m * Hlow) & (h - 1);
-                const uint2 tw = __ldg(&w[h + jj]);
-                uint32_t a = v[u * M + m];
-                a = a >= q2 ? a - q2 : a;
-                const uint32_t b = shoup_mul(v[u * M + m + half], tw.x, tw.y, q);
-                v[u * M + m] = a + b;
-                v[u * M + m + half] = a + q2 - b;
+                const int ti = (m % half) * (16 >> (l + 1));
+                const uint32_t a = v[u * M + m], b = v[u * M + m + half];
+                const uint32_t bw = ti ? shoup_mul(b, T.c16[ti], T.c16q[ti], q) : b;
+                v[u * M + m] = csub(a + bw, q2);
+                v[u * M + m + half] = csub(a + q2 - bw, q2);
             }
         }
+}
+
+__device__ __forceinline__ int brev4(int m) { return ((m & 1) << 3) | ((m & 2) << 1) | ((m & 4) >> 1) | ((m & 8) >> 3); }
+
+// Twiddles of a radix-16 group of a length-N transform, deferred to one factor
+// per slot: slot m of the sub-transform at offset `off` inside blocks of size
+// 2^(lls+4) is multiplied by w_span^(off * bitrev4(m)) = w_N^(off * bitrev4(m) * N/span).
+__device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &T, int off, int lls, int lg)
+{
+    const int sh = lg - lls - 4;   // log2(N / span)
+#pragma unroll
+    for (int m = 1; m < 16; m++) {
+        const uint2 tw = __ldg(&T.w[(off * brev4(m)) << sh]);
+        v[m] = shoup_mul(v[m], tw.x, tw.y, T.q);
     }
 }
 
-__device__ __forceinline__ void regs_to_smem(uint32_t *x, const uint32_t (&v)[16], int t, int G,
-                                             int lls, int span)
+__device__ __forceinline__ void regs_to_smem(uint32_t *x, const uint32_t (&v)[16], int t, int G, int lls, int span)
 {
 #pragma unroll
-    for (int s = 0; s < 16; s++)
-        x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))] = v[s];
+    for (int s = 0; s < 16; s++) x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))] = v[s];
 }
 
-__device__ __forceinline__ void smem_to_regs(uint32_t (&v)[16], const uint32_t *x, int t, int G,
-                                             int lls, int span)
+__device__ __forceinline__ void smem_to_regs(uint32_t (&v)[16], const uint32_t *x, int t, int G, int lls, int span)
 {
 #pragma unroll
-    for (int s = 0; s < 16; s++)
-        v[s] = x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))];
-}
-
-__device__ __forceinline__ void run_dif(uint32_t (&v)[16], int t, int H, int G, const uint2 *w, uint32_t q)
-{
-    switch (G) {
-    case 4: dif_group<4>(v, t, H, w, q); break;
-    case 3: dif_group<3>(v, t, H, w, q); break;
-    case 2: dif_group<2>(v, t, H, w, q); break;
-    default: dif_group<1>(v, t, H, w, q); break;
-    }
-}
-
-__device__ __forceinline__ void run_dit(uint32_t (&v)[16], int t, int Hlow, int G, const uint2 *w, uint32_t q)
-{
-    switch (G) {
-    case 4: dit_group<4>(v, t, Hlow, w, q); break;
-    case 3: dit_group<3>(v, t, Hlow, w, q); break;
-    case 2: dit_group<2>(v, t, Hlow, w, q); break;
-    default: dit_group<1>(v, t, Hlow, w, q); break;
-    }
+    for (int s = 0; s < 16; s++) v[s] = x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))];
 }
 
 // ---------------------------------------------------------------------------
@@ -131,58 +115,64 @@ ntt_fwd_kernel(NttFwdArgs a)
 {
     extern __shared__ uint32_t smem[];
     const int lg = a.lg, N = 1 << lg, TPT = N >> 4;
-    const int tpc = blockDim.x / TPT;
-    const int sub = threadIdx.x / TPT, t = threadIdx.x % TPT;
+    const int tpc = blockDim.x >> (lg - 4);
+    const int sub = threadIdx.x >> (lg - 4), t = threadIdx.x & (TPT - 1);
     const int64_t e = (int64_t)blockIdx.x * tpc + sub;
     const int j = blockIdx.y;
-    const NttDev T = a.tab[j];
+    const NttDev &T = a.tab[j];
     uint32_t *x = smem + sub * (N + (N >> 4));
     const bool active = e < a.nent;
 
-    // first group: 4 stages, elements t + m * N/16
+    // first group: elements t + m * N/16
     uint32_t v[16];
     {
         const uint64_t *src = a.in + (active ? e : 0) * a.in_ld + a.in_off;
-        const int ls = N >> 4;
+        const int L = active ? (int)a.L : 0;
 #pragma unroll
         for (int m = 0; m < 16; m++) {
-            const int d = t + m * ls;
+            const int d = t + m * TPT;
             uint32_t val = 0;
-            if (active && d < a.L) {
+            if (d < L) {
                 const uint64_t s = src[d];
                 val = a.reduce ? mod64_q(s, T.q, T.r32, T.r32q, T.oneq) : (uint32_t)s;
             }
             v[m] = val;
         }
     }
-    const int ngroups = (lg + 3) / 4;
-    int H = N >> 1;
+    const int ngroups = (lg + 3) >> 2;
+    int lgH = lg - 1;
     for (int gi = 0; gi < ngroups; gi++) {
         const int G = (gi < ngroups - 1) ? 4 : lg - 4 * (ngroups - 1);
-        const int lls = (31 - __clz(H)) - (G - 1), span = 2 * H;
+        const int lls = lgH - (G - 1), span = 2 << lgH;
         if (gi > 0) {
             __syncthreads();
             smem_to_regs(v, x, t, G, lls, span);
         }
-        run_dif(v, t, H, G, T.w, T.q);
+        if (G == 4) {
+            dif_const<4>(v, T);
+            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls, lg);
+        } else if (G == 3) {
+            dif_const<3>(v, T);
+        } else if (G == 2) {
+            dif_const<2>(v, T);
+        } else {
+            dif_const<1>(v, T);
+        }
         if (gi < ngroups - 1) {
-            // the next group reads a different pattern: publish through smem
             __syncthreads();   // everyone done reading the previous layout
             regs_to_smem(x, v, t, G, lls, span);
         }
-        H >>= G;
+        lgH -= G;
     }
-    // last group leaves points 16t .. 16t+15 in v[0..15]
+    // the last group leaves points 16t .. 16t+15 in v[0..15]
     if (active) {
         uint32_t *dst = a.out + j * a.prime_stride + e * kPtTile;
+        const uint32_t q = T.q;
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             uint4 o;
-            o.x = v[4 * c + 0]; o.y = v[4 * c + 1]; o.z = v[4 * c + 2]; o.w = v[4 * c + 3];
-            o.x = o.x >= 2 * T.q ? o.x - 2 * T.q : o.x; o.x = o.x >= T.q ? o.x - T.q : o.x;
-            o.y = o.y >= 2 * T.q ? o.y - 2 * T.q : o.y; o.y = o.y >= T.q ? o.y - T.q : o.y;
-            o.z = o.z >= 2 * T.q ? o.z - 2 * T.q : o.z; o.z = o.z >= T.q ? o.z - T.q : o.z;
-            o.w = o.w >= 2 * T.q ? o.w - 2 * T.q : o.w; o.w = o.w >= T.q ? o.w - T.q : o.w;
+            o.x = csub(v[4 * c + 0], q); o.y = csub(v[4 * c + 1], q);
+            o.z = csub(v[4 * c + 2], q); o.w = csub(v[4 * c + 3], q);
             *reinterpret_cast<uint4 *>(dst + (int64_t)(4 * t + c) * a.tile_stride) = o;
         }
     }
@@ -193,11 +183,11 @@ ntt_inv_kernel(NttInvArgs a)
 {
     extern __shared__ uint32_t smem[];
     const int lg = a.lg, N = 1 << lg, TPT = N >> 4;
-    const int tpc = blockDim.x / TPT;
-    const int sub = threadIdx.x / TPT, t = threadIdx.x % TPT;
+    const int tpc = blockDim.x >> (lg - 4);
+    const int sub = threadIdx.x >> (lg - 4), t = threadIdx.x & (TPT - 1);
     const int64_t e = (int64_t)blockIdx.x * tpc + sub;
     const int j = blockIdx.y;
-    const NttDev T = a.tab[j];
+    const NttDev &T = a.tab[j];
     uint32_t *x = smem + sub * (N + (N >> 4));
     const bool active = e < a.nent;
 
@@ -213,33 +203,39 @@ ntt_inv_kernel(NttInvArgs a)
 #pragma unroll
         for (int m = 0; m < 16; m++) v[m] = 0;
     }
-    const int ngroups = (lg + 3) / 4;
+    const int ngroups = (lg + 3) >> 2;
     const int Gfirst = lg - 4 * (ngroups - 1);
-    int Hlow = 1;
+    int lls = 0;
     for (int gi = 0; gi < ngroups; gi++) {
         const int G = (gi == 0) ? Gfirst : 4;
-        const int span = Hlow << G;
-        const int lls = 31 - __clz(Hlow);
+        const int span = 1 << (lls + G);
         if (gi > 0) {
             __syncthreads();
             smem_to_regs(v, x, t, G, lls, span);
         }
-        run_dit(v, t, Hlow, G, T.w, T.q);
+        if (G == 4) {
+            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls, lg);
+            dit_const<4>(v, T);
+        } else if (G == 3) {
+            dit_const<3>(v, T);
+        } else if (G == 2) {
+            dit_const<2>(v, T);
+        } else {
+            dit_const<1>(v, T);
+        }
         if (gi < ngroups - 1) {
             __syncthreads();
             regs_to_smem(x, v, t, G, lls, span);
         }
-        Hlow <<= G;
+        lls += G;
     }
     // last group: element m of thread t is coefficient t + m * N/16
     if (!active) return;
-    const int ls = N >> 4;
 #pragma unroll
     for (int m = 0; m < 16; m++) {
-        const int64_t d = t + m * ls - a.lo;
+        const int64_t d = t + m * TPT - a.lo;
         if (d < 0 || d >= a.cnt) continue;
-        uint32_t val = shoup_mul(v[m], T.ninv, T.ninvq, T.q);
-        val = val >= T.q ? val - T.q : val;
+        const uint32_t val = csub(shoup_mul(v[m], T.ninv, T.ninvq, T.q), T.q);
         if (a.direct)
             a.out64[e * a.out_ld + d] = val;
         else

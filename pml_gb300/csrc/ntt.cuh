@@ -8,12 +8,26 @@ namespace pmlg {
 constexpr int kMaxLgN = 14;
 constexpr int kMinLgN = 4;
 
-// Device view of one NttTable.
+// Device view of one NttTable, for one direction.
 struct NttDev
 {
-    const uint2 *w;      // forward or inverse twiddles (by kernel)
+    const uint2 *w;      // powers of the (forward or inverse) root, with quotients
     uint32_t q, ninv, ninvq, r32, r32q, oneq;
+    uint32_t c16[8], c16q[8];   // (forward or inverse) sixteenth roots of unity
 };
+
+inline NttDev ntt_dev(const NttTable *t, bool inverse)
+{
+    NttDev d;
+    d.w = inverse ? t->d_iw : t->d_w;
+    d.q = t->q; d.ninv = t->ninv; d.ninvq = t->ninvq;
+    d.r32 = t->r32; d.r32q = t->r32q; d.oneq = t->oneq;
+    for (int j = 0; j < 8; j++) {
+        d.c16[j] = inverse ? t->ic16[j] : t->c16[j];
+        d.c16q[j] = inverse ? t->ic16q[j] : t->c16q[j];
+    }
+    return d;
+}
 
 // Evaluations are stored "point-tiled": for prime j, point t and matrix entry e,
 //   E[j * prime_stride + (t / 4) * tile_stride + e * 4 + (t % 4)],

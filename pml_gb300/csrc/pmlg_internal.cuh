@@ -60,14 +60,17 @@ __host__ __device__ __forceinline__ uint32_t mod64_q(uint64_t x, uint32_t q, uin
 // NTT tables
 // ---------------------------------------------------------------------------
 
-// Twiddles for one (prime, N): for each radix-2 stage of half size h, the
-// entries [h, 2h) hold w_{2h}^j (forward) or w_{2h}^{-j} (inverse), j < h.
+// Twiddles for one (prime, N), w a primitive N-th root of unity mod q:
+// d_w[e] = {w^e, Shoup quotient}, d_iw[e] = {w^-e, quotient}, e < N, plus the
+// eighth... sixteenth roots w^(jN/16), j < 8, that the radix-16 butterflies use.
 struct NttTable
 {
     uint32_t q;
     int lg;            // N = 2^lg
-    uint2 *d_w;        // [N] forward twiddles {w, Shoup quotient}
-    uint2 *d_iw;       // [N] inverse twiddles {w, Shoup quotient}
+    uint2 *d_w;        // [N] forward powers
+    uint2 *d_iw;       // [N] inverse powers
+    uint32_t c16[8], c16q[8];      // w^(jN/16) and quotients
+    uint32_t ic16[8], ic16q[8];    // w^(-jN/16) and quotients
     uint32_t ninv, ninvq;    // N^{-1} mod q and quotient
     uint32_t r32, r32q;      // 2^32 mod q and quotient
     uint32_t oneq;           // floor(2^32 / q)

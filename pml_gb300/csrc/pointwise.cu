@@ -223,6 +223,117 @@ pw_i8_kernel(PwArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// CUDA-core form, pipelined: a persistent CTA of 512 threads walks over pairs
+// of points; 256 threads compute each point (4 x 4 outputs per thread) while
+// cp.async brings the next pair into the other half of a two-stage shared
+// memory ring, so global loads overlap the multiply-accumulate.
+// ---------------------------------------------------------------------------
+
+constexpr int CC2_THREADS = 512;
+constexpr int CC2_PLANE = 64 * CC_LD;                 // one 64 x 64 matrix, padded rows
+constexpr int CC2_STAGE = 2 * 2 * CC2_PLANE;          // 2 points x (A, B)
+
+__device__ __forceinline__ void cp_async4(uint32_t *smem_dst, const uint32_t *gsrc)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+__global__ void __launch_bounds__(CC2_THREADS, 1)
+pw_cc2_kernel(PwArgs a)
+{
+    extern __shared__ uint32_t sm[];
+    const int tid = threadIdx.x;
+    const int lg = ilog2_small(a.pt_tile);
+    const int64_t items = (a.npts + 1) >> 1;
+
+    // zero both stages once: the padding outside r x k / k x c stays zero
+    for (int idx = tid; idx < 2 * CC2_STAGE; idx += CC2_THREADS) sm[idx] = 0;
+    __syncthreads();
+
+    auto issue = [&](int64_t item, int stage) {
+        uint32_t *base = sm + stage * CC2_STAGE;
+        const int64_t pt0 = item * 2;
+        for (int idx = tid; idx < 2 * 4096; idx += CC2_THREADS) {
+            const int p = idx >> 12, e = idx & 4095, i = e >> 6, l = e & 63;
+            const int64_t pt = pt0 + p;
+            if (pt >= a.npts) continue;
+            uint32_t *As = base + p * 2 * CC2_PLANE;
+            uint32_t *Bs = As + CC2_PLANE;
+            if (i < a.r && l < a.k)
+                cp_async4(&As[i * CC_LD + l], &a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)]);
+            if (i < a.k && l < a.c)
+                cp_async4(&Bs[i * CC_LD + l], &a.B.base[pw_off(pt, (int64_t)i * a.B.ld + l, lg, a.B.s_tile, a.s_e, a.s_p)]);
+        }
+    };
+
+    const int pl = tid >> 8, ltid = tid & 255, ti = ltid >> 4, tj = ltid & 15;
+    const int kk = (a.k + 7) & ~7;
+    int64_t item = blockIdx.x;
+    if (item < items) issue(item, 0);
+    cp_async_commit();
+    int stage = 0;
+    for (; item < items; item += gridDim.x, stage ^= 1) {
+        const int64_t next = item + gridDim.x;
+        if (next < items) issue(next, stage ^ 1);
+        cp_async_commit();
+        cp_async_wait1();
+        __syncthreads();
+
+        const int64_t pt = item * 2 + pl;
+        if (pt < a.npts) {
+            const uint32_t *Ap = sm + stage * CC2_STAGE + pl * 2 * CC2_PLANE;
+            const uint32_t *Bp = Ap + CC2_PLANE;
+            uint64_t acc[4][4];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int v = 0; v < 4; v++) acc[u][v] = 0;
+            for (int l0 = 0; l0 < kk; l0 += 8) {
+#pragma unroll
+                for (int l = l0; l < l0 + 8; l++) {
+                    uint32_t av[4];
+#pragma unroll
+                    for (int u = 0; u < 4; u++) av[u] = Ap[(4 * ti + u) * CC_LD + l];
+                    const uint4 bv = *reinterpret_cast<const uint4 *>(&Bp[l * CC_LD + 4 * tj]);
+                    const uint32_t b4[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+                    for (int u = 0; u < 4; u++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) acc[u][v] += (uint64_t)av[u] * b4[v];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++)
+                        acc[u][v] = (acc[u][v] >> 32) * (uint64_t)a.r32 + (acc[u][v] & 0xffffffffull);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int i = 4 * ti + u;
+                if (i >= a.r) continue;
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int j = 4 * tj + v;
+                    if (j >= a.c) continue;
+                    uint32_t res = mod64_q(acc[u][v], a.q, a.r32, a.r32q, a.oneq);
+                    const int64_t off = pw_off(pt, (int64_t)i * a.ldc + j, lg, a.s_tile_c, a.s_e, a.s_p);
+                    if (a.accumulate) {
+                        res += a.C[off];
+                        res = res >= a.q ? res - a.q : res;
+                    }
+                    a.C[off] = res;
+                }
+            }
+        }
+        __syncthreads();   // this stage is refilled two items later
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -247,11 +358,11 @@ static int form_resolve(int form)
 int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
 {
     static bool attr_done = false;
-    const size_t smem_cc = 2ull * PW_PPC * 64 * CC_LD * sizeof(uint32_t);
     const size_t smem_i8 = (size_t)PW_PPC * 8 * 64 * I8_LD;
+    const size_t smem_cc2 = 2ull * CC2_STAGE * sizeof(uint32_t);
     if (!attr_done) {
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_i8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i8));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc2));
         attr_done = true;
     }
     if (a.npts <= 0) return PMLG_OK;
@@ -261,8 +372,10 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
         prof_begin(ctx, "pointwise_int8_tc", st);
         pw_i8_kernel<<<(unsigned)grid, PW_THREADS, smem_i8, st>>>(a);
     } else {
+        const int64_t items = (a.npts + 1) / 2;
+        const int64_t g2 = items < ctx->sm_count ? items : ctx->sm_count;
         prof_begin(ctx, "pointwise_cuda_core", st);
-        pw_cc_kernel<<<(unsigned)grid, PW_THREADS, smem_cc, st>>>(a);
+        pw_cc2_kernel<<<(unsigned)g2, CC2_THREADS, smem_cc2, st>>>(a);
     }
     prof_end(ctx, st);
     count_launch(ctx);

@@ -56,8 +56,7 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
     fa.t = t;
     fa.reduce = !plan.direct;
     for (int i = 0; i < t; i++)
-        fa.tab[i] = NttDev{tabs[i]->d_w, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
-                           tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
+        fa.tab[i] = ntt_dev(tabs[i], false);
     // A
     fa.in = j.A; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = nA;
     fa.out = EA; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
@@ -91,8 +90,7 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
     ia.res32 = R32;
     ia.lg = j.lg; ia.t = t; ia.direct = plan.direct;
     for (int i = 0; i < t; i++)
-        ia.tab[i] = NttDev{tabs[i]->d_iw, tabs[i]->q, tabs[i]->ninv, tabs[i]->ninvq,
-                           tabs[i]->r32, tabs[i]->r32q, tabs[i]->oneq};
+        ia.tab[i] = ntt_dev(tabs[i], true);
     PMLG_TRY(ntt_inverse(ctx, ia, st));
     if (!plan.direct) PMLG_TRY(crt_combine(ctx, plan, R32, nC, j.cnt, j.C, j.ldc, j.c_cap, st));
     return PMLG_OK;
