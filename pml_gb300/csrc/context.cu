@@ -137,25 +137,42 @@ int get_table(pmlg_ctx *ctx, uint32_t q, int lg, const NttTable **out)
             return PMLG_EINVAL;
         }
     }
+    // group twiddle tables (layout in pmlg_internal.cuh), copied out of the power tables
+    const uint64_t G = 15 * (N >> 3);   // >= 15 * (2^(lg-3) - 1) entries per direction
+    uint32_t *hg = (uint32_t *)calloc(4 * G, sizeof(uint32_t));
+    if (!hg) { free(hw); return PMLG_ENOMEM; }
+    for (int lls = 0; lls <= lg - 4; lls++) {
+        const uint64_t L = 1ull << lls, base = 15 * (L - 1);
+        for (uint64_t m = 1; m < 16; m++) {
+            const uint64_t br = ((m & 1) << 3) | ((m & 2) << 1) | ((m & 4) >> 1) | ((m & 8) >> 3);
+            for (uint64_t off = 0; off < L; off++) {
+                const uint64_t ex = (off * br) << (lg - lls - 4);   // < N
+                const uint64_t i = base + (m - 1) * L + off;
+                hg[2 * i] = hf[2 * ex]; hg[2 * i + 1] = hf[2 * ex + 1];
+                hg[2 * G + 2 * i] = hi[2 * ex]; hg[2 * G + 2 * i + 1] = hi[2 * ex + 1];
+            }
+        }
+    }
+    free(hw);
     NttTable T;
     T.q = q;
     T.lg = lg;
     void *d = nullptr;
-    cudaError_t e = cudaMalloc(&d, 4 * N * sizeof(uint32_t));
+    cudaError_t e = cudaMalloc(&d, 4 * G * sizeof(uint32_t));
     if (e != cudaSuccess) {
-        free(hw);
+        free(hg);
         set_error(ctx, "cudaMalloc tables: %s", cudaGetErrorString(e));
         return PMLG_ENOMEM;
     }
-    e = cudaMemcpy(d, hw, 4 * N * sizeof(uint32_t), cudaMemcpyHostToDevice);
-    free(hw);
+    e = cudaMemcpy(d, hg, 4 * G * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    free(hg);
     if (e != cudaSuccess) {
         cudaFree(d);
         set_error(ctx, "cudaMemcpy tables: %s", cudaGetErrorString(e));
         return PMLG_ECUDA;
     }
     T.d_w = (uint2 *)d;
-    T.d_iw = T.d_w + N;
+    T.d_iw = T.d_w + G;
     for (int j = 0; j < 8; j++) {
         const uint64_t ex = (uint64_t)j * (N / 16);
         T.c16[j] = (uint32_t)h_powmod(wN, ex, q);

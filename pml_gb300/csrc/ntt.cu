@@ -83,15 +83,16 @@ __device__ __forceinline__ void dit_const(uint32_t (&v)[16], const NttDev &T)
 
 __device__ __forceinline__ int brev4(int m) { return ((m & 1) << 3) | ((m & 2) << 1) | ((m & 4) >> 1) | ((m & 8) >> 3); }
 
-// Twiddles of a radix-16 group of a length-N transform, deferred to one factor
-// per slot: slot m of the sub-transform at offset `off` inside blocks of size
-// 2^(lls+4) is multiplied by w_span^(off * bitrev4(m)) = w_N^(off * bitrev4(m) * N/span).
-__device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &T, int off, int lls, int lg)
+// Twiddles of a radix-16 group, deferred to one factor per slot: slot m of
+// the sub-transform at offset `off` inside blocks of size 2^(lls+4) is
+// multiplied by w_span^(off * bitrev4(m)), read from the group table of size
+// 2^lls (consecutive offs are consecutive entries: coalesced).
+__device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &T, int off, int lls)
 {
-    const int sh = lg - lls - 4;   // log2(N / span)
+    const uint2 *g = T.w + 15 * ((1 << lls) - 1) + off;
 #pragma unroll
     for (int m = 1; m < 16; m++) {
-        const uint2 tw = __ldg(&T.w[(off * brev4(m)) << sh]);
+        const uint2 tw = __ldg(&g[(m - 1) << lls]);
         v[m] = shoup_mul(v[m], tw.x, tw.y, T.q);
     }
 }
@@ -150,7 +151,7 @@ ntt_fwd_kernel(NttFwdArgs a)
         }
         if (G == 4) {
             dif_const<4>(v, T);
-            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls, lg);
+            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls);
         } else if (G == 3) {
             dif_const<3>(v, T);
         } else if (G == 2) {
@@ -214,7 +215,7 @@ ntt_inv_kernel(NttInvArgs a)
             smem_to_regs(v, x, t, G, lls, span);
         }
         if (G == 4) {
-            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls, lg);
+            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls);
             dit_const<4>(v, T);
         } else if (G == 3) {
             dit_const<3>(v, T);

@@ -11,7 +11,7 @@ constexpr int kMinLgN = 4;
 // Device view of one NttTable, for one direction.
 struct NttDev
 {
-    const uint2 *w;      // powers of the (forward or inverse) root, with quotients
+    const uint2 *w;      // group twiddle table of the direction (layout: NttTable)
     uint32_t q, ninv, ninvq, r32, r32q, oneq;
     uint32_t c16[8], c16q[8];   // (forward or inverse) sixteenth roots of unity
 };

@@ -60,15 +60,19 @@ __host__ __device__ __forceinline__ uint32_t mod64_q(uint64_t x, uint32_t q, uin
 // NTT tables
 // ---------------------------------------------------------------------------
 
-// Twiddles for one (prime, N), w a primitive N-th root of unity mod q:
-// d_w[e] = {w^e, Shoup quotient}, d_iw[e] = {w^-e, quotient}, e < N, plus the
-// eighth... sixteenth roots w^(jN/16), j < 8, that the radix-16 butterflies use.
+// Twiddles for one (prime, N), w a primitive N-th root of unity mod q.
+// The radix-16 groups of the NTT need, for a group whose sub-transforms are
+// spaced L = 2^lls apart (span 16L), the factors w_span^(off * bitrev4(m)) for
+// off < L and m = 1..15.  They are stored per group size, coalesced over off:
+//   d_w[15 (2^lls - 1) + (m - 1) 2^lls + off] = {w^(off bitrev4(m) N / 16L), quotient}
+// (d_iw: the same with w^-1), lls = 0 .. lg-4, fewer than 2N entries each.
+// c16 holds the sixteenth roots w^(jN/16), j < 8, of the butterflies.
 struct NttTable
 {
     uint32_t q;
     int lg;            // N = 2^lg
-    uint2 *d_w;        // [N] forward powers
-    uint2 *d_iw;       // [N] inverse powers
+    uint2 *d_w;        // forward group twiddles
+    uint2 *d_iw;       // inverse group twiddles
     uint32_t c16[8], c16q[8];      // w^(jN/16) and quotients
     uint32_t ic16[8], ic16q[8];    // w^(-jN/16) and quotients
     uint32_t ninv, ninvq;    // N^{-1} mod q and quotient
