@@ -196,6 +196,27 @@ PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t
                                      const uint64_t *v, int64_t len, int64_t k, uint64_t p,
                                      void *stream);
 
+/* pmlg_nmod_vec_dot_multi without any allocation.  This entry point has no
+ * counterpart in the reference; it exists for callers that cannot allocate
+ * device memory at the point of the call.  Examples: code that runs under a
+ * device-memory budget fixed up front by another allocator, or a pipeline
+ * that must not hit the implicit device synchronisation of cudaMalloc/cudaFree
+ * in the middle of its work.  It takes no pmlg_ctx.  The partial sums go to a
+ * file-scope device array of 65536 x 24 bytes (1.5 MiB), which every GPU that
+ * loads the library holds until the process exits.
+ * Device pointers; computes the same uv[j] = sum_i u[i] v[i*k + j] mod p as
+ * pmlg_nmod_vec_dot_multi, on the current device.
+ * - k may be at most 65536; larger k returns PMLG_EUNSUP and nothing runs.
+ * - The first call on a device looks up the array's device address
+ *   (cudaGetSymbolAddress) with that device current.  Make that first call
+ *   before any stream capture.
+ * - Every call shares the one array.  Calls that overlap on the GPU (on
+ *   different streams, or from different threads) race on it and must be
+ *   serialised by the caller.  No state carries over from one call to the
+ *   next: every partial sum a call reads, that call wrote first. */
+PMLG_API int pmlg_nmod_vec_dot_multi_noalloc(uint64_t *uv, const uint64_t *u, const uint64_t *v,
+                                             int64_t len, int64_t k, uint64_t p, void *stream);
+
 /* residues[j*nb + i] = input[i] mod primes[j], j < nprimes <= 6, primes < 2^63:
  * replaces nmod_multimod_CRT_reduce (flint-extras/src/nmod_extra/nmod_multimod_CRT_reduce.c:22). */
 PMLG_API int pmlg_multimod_reduce(pmlg_ctx *ctx, uint64_t *residues, const uint64_t *input,

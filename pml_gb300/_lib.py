@@ -48,6 +48,7 @@ SIGNATURES = {
     "pmlg_nmod32_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
     "pmlg_nmod32_vec_mdot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _u64, _vp]),
     "pmlg_nmod_vec_dot_multi": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _i64, _u64, _vp]),
+    "pmlg_nmod_vec_dot_multi_noalloc": (C.c_int, [_vp, _vp, _vp, _i64, _i64, _u64, _vp]),
     "pmlg_multimod_reduce": (C.c_int, [_vp, _vp, _vp, _i64, _vp, C.c_int, _vp]),
     "pmlg_multimod_crt": (C.c_int, [_vp, _vp, _vp, _i64, _vp, C.c_int, _u64, _vp]),
 }

@@ -10,6 +10,8 @@
 // limits.
 #include "pmlg_internal.cuh"
 
+#include <mutex>
+
 namespace pmlg {
 
 struct U192
@@ -328,6 +330,77 @@ PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t
     prof_end(ctx, st);
     count_launch(ctx, 2);
     PMLG_CUDA_TRY(cudaGetLastError());
+    return PMLG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Vector-matrix dot product without any allocation
+// ---------------------------------------------------------------------------
+//
+// Same kernels as pmlg_nmod_vec_dot_multi, but the partial sums live in a
+// file-scope device array instead of context scratch, so the call needs no
+// pmlg_ctx and never calls cudaMalloc/cudaFree.  The array is part of the
+// library's device image: every GPU that loads the library holds its
+// kNoAllocPartials * 24 bytes (1.5 MiB) until the process exits.
+
+namespace pmlg {
+
+constexpr int64_t kNoAllocPartials = 65536;   // largest number of columns k
+static __device__ __align__(256) U192 g_noalloc_partials[kNoAllocPartials];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static U192 *g_noalloc_ptr[kNoAllocMaxDevices];   // device address of the array, per device
+static int g_noalloc_sms[kNoAllocMaxDevices];
+
+}  // namespace pmlg
+
+extern "C" {
+
+PMLG_API int pmlg_nmod_vec_dot_multi_noalloc(uint64_t *uv, const uint64_t *u, const uint64_t *v, int64_t len,
+                                             int64_t k, uint64_t p, void *stream)
+{
+    if (len < 0 || k < 0) return PMLG_EINVAL;
+    if (k == 0) return PMLG_OK;
+    if (!uv || (len > 0 && (!u || !v))) return PMLG_EINVAL;
+    if (p < 2) return PMLG_EBADMOD;
+    if (k > kNoAllocPartials) return PMLG_EUNSUP;   // the fixed scratch holds at most this many columns
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PMLG_ECUDA;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return PMLG_EUNSUP;
+    U192 *part = nullptr;
+    int sms = 0;
+    {
+        // first call on this device: resolve the array's device address with the
+        // device current (host code cannot use the symbol itself as a pointer)
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_ptr[dev]) {
+            void *addr = nullptr;
+            if (cudaGetSymbolAddress(&addr, g_noalloc_partials) != cudaSuccess || !addr) return PMLG_ECUDA;
+            int n = 0;
+            if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return PMLG_ECUDA;
+            g_noalloc_sms[dev] = n;
+            g_noalloc_ptr[dev] = (U192 *)addr;
+        }
+        part = g_noalloc_ptr[dev];
+        sms = g_noalloc_sms[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    const int threads = 128;
+    const int64_t gx = (k + threads - 1) / threads;
+    int64_t nchunks = ((int64_t)sms * 8 + gx - 1) / gx;
+    if (nchunks > (len + 63) / 64) nchunks = (len + 63) / 64;
+    if (nchunks > kNoAllocPartials / k) nchunks = kNoAllocPartials / k;   // nchunks * k partials fit
+    if (nchunks > 65535) nchunks = 65535;
+    if (nchunks < 1) nchunks = 1;
+    const int64_t chunk = (len + nchunks - 1) / nchunks > 0 ? (len + nchunks - 1) / nchunks : 1;
+    // every partial that dot_multi_final reads is written by dot_multi_partial in
+    // this same call, so nothing left in the array by an earlier call is used
+    dot_multi_partial<<<dim3((unsigned)gx, (unsigned)nchunks), threads, 0, st>>>(u, v, len, k, chunk, part);
+    dot_multi_final<<<(unsigned)gx, threads, 0, st>>>(part, nchunks, k, p, uv);
+    if (cudaGetLastError() != cudaSuccess) return PMLG_ECUDA;
     return PMLG_OK;
 }
 
