@@ -58,7 +58,7 @@ def parse():
 
 
 def run_profile_case(args):
-    """One headline product with each form (INT8 first), or one pmbasis 64x32 at
+    """One headline product with each form (FP16 digits, INT8, CUDA cores), or one pmbasis 64x32 at
     order 1024: a short, fixed launch sequence for profiler captures."""
     import torch
     import pml_gb300
@@ -68,11 +68,12 @@ def run_profile_case(args):
         dA = torch.from_numpy(A.view(np.int64)).cuda()
         dB = torch.from_numpy(B.view(np.int64)).cuda()
         outs = []
-        for form in (pml_gb300.FORM_INT8_TC, pml_gb300.FORM_CUDA_CORE):
+        for form in (pml_gb300.FORM_F16_TC, pml_gb300.FORM_INT8_TC, pml_gb300.FORM_CUDA_CORE):
             ctx.set_form(form)
             outs.append(pml_gb300.nmod_poly_mat_multiply(dA, dB, P, ctx=ctx))
         torch.cuda.synchronize()
-        print(json.dumps({"profile_case": "product", "forms_agree": bool(torch.equal(outs[0], outs[1])),
+        print(json.dumps({"profile_case": "product",
+                          "forms_agree": all(bool(torch.equal(outs[0], o)) for o in outs),
                           "launches": ctx.launches}))
     else:
         rng = np.random.default_rng(7)
@@ -212,6 +213,8 @@ def algorithmic_bytes(kernel: str):
         return ("hbm", R * C * (N * 4 + (2 * LEN - 1) * 8))  # read evaluations, write uint64 coefficients
     if kernel == "pointwise_int8_tc":
         return ("tensor", 2 * 16 * N * R * K * C)           # 16 limb products per MAC, 2 ops per MAC
+    if kernel == "pointwise_f16_tc":
+        return ("tensor", 2 * 12 * N * R * K * C)           # 12 digit products per MAC on FP16 tensor cores
     if kernel == "pointwise_cuda_core":
         return ("hbm", 3 * N * R * C * 4)
     return ("hbm", None)
@@ -275,18 +278,24 @@ def run_pml(args):
         ms = e0.elapsed_time(e1) / steps
         return max_over_ranks(ms), ctx.launches - l0, (sampler.summary() if sampler else None)
 
-    # correctness spot-check of this exact workload before timing: both forms equal
-    ctx.set_form(pml_gb300.FORM_CUDA_CORE)
-    step()
-    ref = dC.clone()
-    ctx.set_form(pml_gb300.FORM_INT8_TC)
-    step()
-    torch.cuda.synchronize()
-    forms_agree = bool(torch.equal(ref, dC))
-    del ref
+    FORMS = (("f16_tc", pml_gb300.FORM_F16_TC), ("int8_tc", pml_gb300.FORM_INT8_TC),
+             ("cuda_core", pml_gb300.FORM_CUDA_CORE))
+    HEAD = pml_gb300.FORM_F16_TC
 
-    ms_i8, launches, clocks = timed(pml_gb300.FORM_INT8_TC, args.steps, args.warmup, clocks=True)
-    ms_cc, _, _ = timed(pml_gb300.FORM_CUDA_CORE, args.steps, args.warmup)
+    # correctness spot-check of this exact workload before timing: all forms equal
+    outs_chk = {}
+    for name, form in FORMS:
+        ctx.set_form(form)
+        step()
+        outs_chk[name] = dC.clone()
+    torch.cuda.synchronize()
+    forms_agree = all(bool(torch.equal(outs_chk["cuda_core"], v)) for v in outs_chk.values())
+    del outs_chk
+
+    ms = {}
+    ms["f16_tc"], launches, clocks = timed(HEAD, args.steps, args.warmup, clocks=True)
+    ms["int8_tc"], _, _ = timed(pml_gb300.FORM_INT8_TC, args.steps, args.warmup)
+    ms["cuda_core"], _, _ = timed(pml_gb300.FORM_CUDA_CORE, args.steps, args.warmup)
 
     # per-kernel device times (separate pass, events on the launch stream)
     def kernel_profile(form: int, steps: int):
@@ -301,17 +310,16 @@ def run_pml(args):
         ctx.set_profiling(False)
         return prof
 
-    prof_i8 = kernel_profile(pml_gb300.FORM_INT8_TC, args.steps)
-    prof_cc = kernel_profile(pml_gb300.FORM_CUDA_CORE, args.steps)
+    profs = {name: kernel_profile(form, args.steps) for name, form in FORMS}
 
     def summarize(prof):
         tot = sum(v[0] for v in prof.values()) or 1.0
         return {k: {"ms_per_launch": v[0] / v[1], "launches": v[1], "share": v[0] / tot} for k, v in prof.items()}
 
-    kern_i8 = summarize(prof_i8)
-    dom = max(prof_i8, key=lambda k: prof_i8[k][0])
+    prof_h = profs["f16_tc"]
+    dom = max(prof_h, key=lambda k: prof_h[k][0])
     bound, work = algorithmic_bytes(dom)
-    avg_s = prof_i8[dom][0] / prof_i8[dom][1] / 1e3
+    avg_s = prof_h[dom][0] / prof_h[dom][1] / 1e3
     peaks = {}
     pk = ROOT / "MEASURED_PEAKS.json"
     if pk.exists():
@@ -330,14 +338,14 @@ def run_pml(args):
             ach = work / avg_s / 1e12
             roofline = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                         "frac": ach / peak, "traffic": None,
-                        "peak_source": "measured dense bf16 (no measured INT8 peak exists for this pool)",
+                        "peak_source": "measured dense bf16 (burst)" if "bf16_tflops" in peaks else "fallback",
                         "algorithmic_ops_per_launch": work}
 
     # end to end through the host-buffer entry point, pinned host memory
     hA = torch.from_numpy(A.view(np.int64)).pin_memory()
     hB = torch.from_numpy(B.view(np.int64)).pin_memory()
     hC = torch.empty((R, C, 2 * LEN - 1), dtype=torch.int64).pin_memory()
-    ctx.set_form(pml_gb300.FORM_INT8_TC)
+    ctx.set_form(HEAD)
 
     def e2e_step():
         ctx.check(ctx.lib.pmlg_poly_mat_mul_host(ctx.handle, hC.data_ptr(), hA.data_ptr(), hB.data_ptr(),
@@ -366,7 +374,7 @@ def run_pml(args):
         dF = torch.from_numpy(F.view(np.int64)).to(dev)
         pm = {}
         outs = {}
-        for name, form in (("int8_tc", pml_gb300.FORM_INT8_TC), ("cuda_core", pml_gb300.FORM_CUDA_CORE)):
+        for name, form in FORMS:
             ctx.set_form(form)
             pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
             torch.cuda.synchronize()
@@ -376,14 +384,15 @@ def run_pml(args):
             pm[name + "_ms"] = max_over_ranks((time.perf_counter() - t0) * 1e3)
             outs[name] = (ab, sh)
         ctx.set_profiling(True)
-        ctx.set_form(pml_gb300.FORM_INT8_TC)
+        ctx.set_form(HEAD)
         pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
         prof = ctx.profile()
         ctx.set_profiling(False)
-        pm["kernels_int8_tc"] = summarize(prof)
-        pm["forms_agree"] = bool(torch.equal(outs["int8_tc"][0], outs["cuda_core"][0])
-                                 and list(outs["int8_tc"][1]) == list(outs["cuda_core"][1]))
-        pm["speedup_int8_vs_cuda_core"] = pm["cuda_core_ms"] / pm["int8_tc_ms"]
+        pm["kernels_f16_tc"] = summarize(prof)
+        pm["forms_agree"] = all(bool(torch.equal(outs["cuda_core"][0], v[0])) and list(v[1]) == list(outs["cuda_core"][1])
+                                for v in outs.values())
+        pm["speedup_f16_tc_vs_cuda_core"] = pm["cuda_core_ms"] / pm["f16_tc_ms"]
+        pm["speedup_int8_tc_vs_cuda_core"] = pm["cuda_core_ms"] / pm["int8_tc_ms"]
         pm["config"] = "pmbasis 64x32, order 8192, zero shift, p = 998244353, uniform coefficients"
         pm["timing"] = "wall clock around one call (it synchronises internally), after one warm-up call"
 
@@ -396,18 +405,22 @@ def run_pml(args):
 
     if rank == 0:
         line = {
-            "metric": METRIC, "value": ms_i8, "unit": "ms", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_i8, "higher_is_better": False, "scaling": "weak",
+            "metric": METRIC, "value": ms["f16_tc"], "unit": "ms", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms["f16_tc"], "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded uniform [0,p), numpy PCG64)",
-            "config": {"workload": WORKLOAD, "form": "int8_tc (mma.sync u8 limbs, s32 accumulate)",
+            "config": {"workload": WORKLOAD,
+                       "form": "f16_tc: exact split-digit tensor-core form (tcgen05 kind::f16, FP32 accumulate); "
+                               "the INT8 split-limb form (mma.sync, GB300's legacy INT8 rate) is timed beside it",
                        "parallelism": f"replicas x{world}", "l2": "inputs 268 MB > 129 MB L2, no flush",
                        "transform": "N = 8192, 2 x 4096 forward + 4096 inverse NTTs"},
-            "cuda_core_ms": ms_cc, "speedup_int8_vs_cuda_core": ms_cc / ms_i8, "forms_agree": forms_agree,
+            "forms_ms": ms, "forms_agree": forms_agree,
+            "speedup_f16_tc_vs_cuda_core": ms["cuda_core"] / ms["f16_tc"],
+            "speedup_int8_tc_vs_cuda_core": ms["cuda_core"] / ms["int8_tc"],
             "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "path": "pmlg_poly_mat_mul_host, pinned host buffers", "matches_device": e2e_ok},
             "gpu_launches": launches,
             "roofline": roofline,
-            "kernels": {"int8_tc": kern_i8, "cuda_core": summarize(prof_cc)},
+            "kernels": {name: summarize(pr) for name, pr in profs.items()},
             "clocks": clocks,
             "pmbasis": pm,
             "cpu_baseline": cpu,

@@ -53,7 +53,9 @@ enum pmlg_form
 {
     PMLG_FORM_AUTO = 0,       /* library choice (fastest measured) */
     PMLG_FORM_CUDA_CORE = 1,  /* uint64 multiply-accumulate with delayed reduction */
-    PMLG_FORM_INT8_TC = 2     /* 8-bit limbs on the INT8 tensor cores (mma.sync, s32 accumulate) */
+    PMLG_FORM_INT8_TC = 2,    /* 8-bit limbs on the INT8 tensor cores (mma.sync, s32 accumulate) */
+    PMLG_FORM_F16_TC = 3      /* exact small signed digits in FP16 on tcgen05 (FP32 accumulate, all
+                                 partial sums below 2^22 so every step is exact) */
 };
 
 /* ---------------------------------------------------------------------- */

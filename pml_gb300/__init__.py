@@ -24,10 +24,10 @@ from typing import Optional
 import numpy as np
 
 from . import _lib
-from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_INT8_TC, PmlgError, PolymatJob, check
+from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_F16_TC, FORM_INT8_TC, PmlgError, PolymatJob, check
 
 __all__ = [
-    "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC",
+    "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
     "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",

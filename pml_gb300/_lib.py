@@ -14,7 +14,7 @@ LIB_PATH = _HERE / "libpmlg.so"
 PMLG_OK = 0
 STATUS = {0: "PMLG_OK", 1: "PMLG_EINVAL", 2: "PMLG_EBADMOD", 3: "PMLG_ENOROOT", 4: "PMLG_ELEN",
           5: "PMLG_EALIAS", 6: "PMLG_ETIMEOUT", 7: "PMLG_ECUDA", 8: "PMLG_ENOMEM", 9: "PMLG_EUNSUP"}
-FORM_AUTO, FORM_CUDA_CORE, FORM_INT8_TC = 0, 1, 2
+FORM_AUTO, FORM_CUDA_CORE, FORM_INT8_TC, FORM_F16_TC = 0, 1, 2, 3
 
 _vp = C.c_void_p
 _i64 = C.c_int64

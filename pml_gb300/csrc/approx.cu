@@ -40,6 +40,7 @@ struct LeafArgs
     int m, n, order;
     uint32_t p, r32, r32q, oneq;
     uint32_t pneg;    // -p^{-1} mod 2^32 (Montgomery reduction)
+    uint32_t r2;      // 2^64 mod p (Montgomery conversion)
 };
 
 __device__ __forceinline__ uint32_t mulmod32(uint32_t a, uint32_t b, const LeafArgs &A)
@@ -267,27 +268,30 @@ mbasis_leaf_kernel(LeafArgs a)
 // ---------------------------------------------------------------------------
 //
 // One leaf runs on a cluster of LC_CL CTAs (one per SM).  CTA c keeps, in its
-// own shared memory, the columns [c*cm, (c+1)*cm) of every coefficient of
-// appbas and the columns [c*cn, (c+1)*cn) of every coefficient of the
+// own shared memory, the columns [c*ncm, (c+1)*ncm) of every coefficient of
+// appbas and the columns [c*ncn, (c+1)*ncn) of every coefficient of the
 // residual R.  Each step:
-//   1. every CTA computes the same stable shift permutation;
+//   1. every CTA computes the same stable shift permutation (rank counting,
+//      8 threads per row);
 //   2. every CTA writes its slice of the permuted R[ord] (transposed) into
 //      CTA 0's shared memory (distributed shared memory stores); cluster barrier;
-//   3. CTA 0 runs the elimination with 4 warps: lane j holds row j of
-//      E = R[ord]^T (j < n <= 32), warp w holds columns [16w, 16w+16) in
+//   3. CTA 0 runs the elimination with its 16 warps: lane j holds row j of
+//      E = R[ord]^T (j < n <= 32), warp w holds columns [4w, 4w+4) in
 //      registers; column c's owner warp finds the pivot with a ballot and
-//      publishes it through shared memory (double-buffered, one named barrier
-//      per column); every warp updates its columns with pivot row values taken
-//      by warp shuffles.  Updates are division-free,
+//      publishes it through shared memory (double-buffered, one barrier per
+//      column); every warp updates its columns with pivot row values taken by
+//      warp shuffles.  Updates are division-free,
 //      row_j <- (pv * row_j - f_j * row_pl) * 2^-32 mod p (Montgomery
 //      reduction): every row operation only scales rows, so the ratios
-//      E[pl_b][np_a] / E[pl_b][pc_b] at the end are the RREF entries;
-//   4. CTA 0 computes X and writes X, the pivot rows and the rank into every
-//      CTA; cluster barrier;
-//   5. every CTA updates its slices (non-pivot rows += X * pivot rows, pivot
-//      rows times x) and the shift.
-// appbas' length is tracked as an upper bound (+1 per step); the output is
-// zero beyond the actual length, which the host reads back.
+//      E[pl_b][np_a] / E[pl_b][pc_b] at the end are the RREF entries.  Once
+//      every row holds a pivot, the remaining columns are non-pivots;
+//   4. CTA 0 computes X (pivot inverses by Montgomery exponentiation), the
+//      pivot rows and the exact appbas length; cluster barrier; every CTA
+//      copies them from CTA 0;
+//   5. every CTA updates its slices (non-pivot rows += X * pivot rows, a
+//      whole row slice per thread; pivot rows times x) and the shift, and
+//      reports to CTA 0 whether a pivot row reached appbas' top coefficient
+//      (the length grows by one when any did, nmod_mat_poly_mbasis.c:306-313).
 
 constexpr int LC_CL = 8;
 constexpr int LC_THREADS = 512;
@@ -302,14 +306,26 @@ __device__ __forceinline__ uint32_t redc(uint64_t t, uint32_t p, uint32_t pneg)
     return r >= p ? r - p : r;
 }
 
-__device__ __forceinline__ void bar_elim() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+// b^e mod p by square and multiply in Montgomery form; r2 = 2^64 mod p
+__device__ __forceinline__ uint32_t mont_pow(uint32_t b, uint32_t e, uint32_t p, uint32_t pneg, uint32_t r2, uint32_t r1)
+{
+    uint32_t xm = redc((uint64_t)b * r2, p, pneg);   // b * 2^32 mod p
+    uint32_t rm = r1;                               // 1 * 2^32 mod p
+    while (e) {
+        if (e & 1) rm = redc((uint64_t)rm * xm, p, pneg);
+        xm = redc((uint64_t)xm * xm, p, pneg);
+        e >>= 1;
+    }
+    return redc(rm, p, pneg);
+}
 
 struct LcShared
 {
     uint32_t E[LC_MAXN][LC_MAXM + 1];   // gathered R[ord]^T (CTA 0)
-    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank (every CTA)
+    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank
     int pivrow[LC_MAXM], nprow[LC_MAXM];
-    int info[2];                        // rank, nullity
+    int info[3];                        // rank, nullity, appbas length for this step's update
+    int growf[LC_CL];                   // CTA 0: per-CTA "pivot row at the top coefficient" flags
     long long sh[LC_MAXM];
     int perm[LC_MAXM];
     uint32_t fbuf[2][32];
@@ -349,17 +365,26 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         AB[idx] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
     }
     if (tid < m) S.sh[tid] = a.shift[tid];
-    int alen = 1;
+    if (tid < LC_CL) S.growf[tid] = 0;
+    if (tid == 0) S.info[2] = 1;
+    int alen = 1;              // exact length of appbas, identical in every CTA
     uint32_t *E0 = cluster.map_shared_rank(&S.E[0][0], 0);
+    int *growf0 = cluster.map_shared_rank(S.growf, 0);
     cluster.sync();
 
     for (int ord = 0; ord < order; ord++) {
-        // 1. stable shift permutation (identical in every CTA)
-        if (tid < m) {
+        // 1. stable shift permutation (identical in every CTA): 8 threads per row
+        if (tid < 8 * LC_MAXM) {
+            const int i = tid >> 3, part = tid & 7;
             int r = 0;
-            const long long v = S.sh[tid];
-            for (int i = 0; i < m; i++) r += (S.sh[i] < v) || (S.sh[i] == v && i < tid);
-            S.perm[r] = tid;
+            if (i < m) {
+                const long long v = S.sh[i];
+                for (int jj = part; jj < m; jj += 8) r += (S.sh[jj] < v) || (S.sh[jj] == v && jj < i);
+            }
+            r += __shfl_xor_sync(0xffffffffu, r, 1);
+            r += __shfl_xor_sync(0xffffffffu, r, 2);
+            r += __shfl_xor_sync(0xffffffffu, r, 4);
+            if (i < m && part == 0) S.perm[r] = i;
         }
         __syncthreads();
         // 2. gather the permuted R[ord]^T into CTA 0
@@ -369,90 +394,103 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         }
         cluster.sync();
 
-        // 3. elimination in CTA 0
-        if (c == 0 && tid < 128) {
+        // 3. elimination in CTA 0 (all 16 warps)
+        if (c == 0) {
             const int w = tid >> 5, lane = tid & 31;
-            uint32_t x[16];
+            uint32_t x[4];
 #pragma unroll
-            for (int k = 0; k < 16; k++) x[k] = (lane < n && 16 * w + k < m) ? S.E[lane][16 * w + k] : 0u;
+            for (int k = 0; k < 4; k++) x[k] = (lane < n && 4 * w + k < m) ? S.E[lane][4 * w + k] : 0u;
             unsigned used = 0;
             int rank = 0, nn = 0;
-            for (int cw = 0; cw < 4; cw++) {
-#pragma unroll
-                for (int cl = 0; cl < 16; cl++) {
-                    const int col = cw * 16 + cl;
-                    if (col >= m) break;
-                    const int buf = col & 1;
-                    if (w == cw) {
-                        const uint32_t v = x[cl];
-                        const unsigned cand =
-                            __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
-                        const int pl = cand ? __ffs(cand) - 1 : -1;
-                        S.fbuf[buf][lane] = v;
-                        if (lane == 0) S.plbuf[buf] = pl;
-                        if (lane == pl) S.pvbuf[buf] = v;
-                    }
-                    bar_elim();
-                    const int pl = S.plbuf[buf];
-                    if (pl < 0) {
-                        if (tid == 0) S.nonpiv[nn] = col;
-                        nn++;
-                        continue;
-                    }
-                    const uint32_t pv = S.pvbuf[buf];
-                    const uint32_t f = S.fbuf[buf][lane];
-                    const uint32_t nf = f ? p - f : 0u;
-#pragma unroll
-                    for (int k = 0; k < 16; k++) {
-                        const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
-                        if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
-                    }
-                    used |= 1u << pl;
-                    if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
-                    rank++;
+            for (int col = 0; col < m; col++) {
+                if (rank == n) {
+                    // every row holds a pivot: the remaining columns are non-pivots
+                    if (tid == 0) S.nonpiv[nn] = col;
+                    nn++;
+                    continue;
                 }
-            }
-#pragma unroll
-            for (int k = 0; k < 16; k++)
-                if (lane < n && 16 * w + k < m) S.E[lane][16 * w + k] = x[k];
-            if (tid == 0) { S.info[0] = rank; S.info[1] = m - rank; }
-        }
-        __syncthreads();
-        if (c == 0) {
-            const int rank = S.info[0], nullity = S.info[1];
-            if (rank > 0 && nullity > 0) {
-                if (tid < rank) {
-                    // Fermat inverse of the pivot value
-                    uint32_t b = S.E[S.pivlane[tid]][S.pivcol[tid]], r = 1;
-                    for (uint32_t e = p - 2; e; e >>= 1) {
-                        if (e & 1) r = mod64_q((uint64_t)r * b, p, a.r32, a.r32q, a.oneq);
-                        b = mod64_q((uint64_t)b * b, p, a.r32, a.r32q, a.oneq);
-                    }
-                    S.inv[tid] = r;
+                const int buf = col & 1, cw = col >> 2, cl = col & 3;
+                if (w == cw) {
+                    uint32_t v = x[0];
+                    if (cl == 1) v = x[1];
+                    if (cl == 2) v = x[2];
+                    if (cl == 3) v = x[3];
+                    const unsigned cand = __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
+                    const int pl = cand ? __ffs(cand) - 1 : -1;
+                    S.fbuf[buf][lane] = v;
+                    if (lane == 0) S.plbuf[buf] = pl;
+                    if (lane == pl) S.pvbuf[buf] = v;
                 }
                 __syncthreads();
-                // X and the row indices, written into every CTA of the cluster
+                const int pl = S.plbuf[buf];
+                if (pl < 0) {
+                    if (tid == 0) S.nonpiv[nn] = col;
+                    nn++;
+                    continue;
+                }
+                const uint32_t pv = S.pvbuf[buf];
+                const uint32_t f = S.fbuf[buf][lane];
+                const uint32_t nf = f ? p - f : 0u;
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
+                    if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
+                }
+                used |= 1u << pl;
+                if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
+                rank++;
+            }
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                if (lane < n && 4 * w + k < m) S.E[lane][4 * w + k] = x[k];
+            __syncthreads();
+            const int nullity = m - rank;
+            if (rank > 0 && nullity > 0) {
+                if (tid < rank) {
+                    S.inv[tid] = mont_pow(S.E[S.pivlane[tid]][S.pivcol[tid]], p - 2, p, a.pneg, a.r2, a.r32);
+                    S.pivrow[tid] = S.perm[S.pivcol[tid]];
+                }
+                if (tid < nullity) S.nprow[tid] = S.perm[S.nonpiv[tid]];
+                __syncthreads();
                 for (int idx = tid; idx < nullity * rank; idx += nth) {
                     const int ia = idx / rank, b = idx - ia * rank;
                     const uint32_t v = mod64_q((uint64_t)S.E[S.pivlane[b]][S.nonpiv[ia]] * S.inv[b], p,
                                                a.r32, a.r32q, a.oneq);
-                    const uint32_t xv = v ? p - v : 0u;
-                    for (int cc = 0; cc < LC_CL; cc++) cluster.map_shared_rank(&S.X[0][0], cc)[ia * LC_MAXM + b] = xv;
-                }
-                for (int idx = tid; idx < LC_CL * m; idx += nth) {
-                    const int cc = idx / m, i = idx - cc * m;
-                    if (i < rank) cluster.map_shared_rank(S.pivrow, cc)[i] = S.perm[S.pivcol[i]];
-                    else cluster.map_shared_rank(S.nprow, cc)[i - rank] = S.perm[S.nonpiv[i - rank]];
+                    S.X[ia][b] = v ? p - v : 0u;
                 }
             }
-            if (tid < LC_CL) {
-                cluster.map_shared_rank(S.info, tid)[0] = rank;
-                cluster.map_shared_rank(S.info, tid)[1] = nullity;
+            if (tid == 0) {
+                S.info[0] = rank;
+                S.info[1] = nullity;
+                // length of appbas after the previous step: it grew if a pivot row
+                // reached the top coefficient in any CTA
+                int g = 0;
+                for (int cc = 0; cc < LC_CL; cc++) g |= S.growf[cc];
+                S.info[2] += g;
             }
         }
         cluster.sync();
 
+        // 4. every CTA takes rank, pivots, X and the length from CTA 0
+        if (c != 0) {
+            const int *info0 = cluster.map_shared_rank(S.info, 0);
+            const int rk = info0[0], nl = info0[1];
+            if (tid < 3) S.info[tid] = info0[tid];
+            if (rk > 0 && nl > 0) {
+                const int *pr0 = cluster.map_shared_rank(S.pivrow, 0);
+                const int *np0 = cluster.map_shared_rank(S.nprow, 0);
+                const uint32_t *X0 = cluster.map_shared_rank(&S.X[0][0], 0);
+                if (tid < rk) S.pivrow[tid] = pr0[tid];
+                if (tid < nl) S.nprow[tid] = np0[tid];
+                for (int idx = tid; idx < nl * rk; idx += nth) {
+                    const int ia = idx / rk, b = idx - ia * rk;
+                    S.X[ia][b] = X0[ia * LC_MAXM + b];
+                }
+            }
+        }
+        __syncthreads();
         const int rank = S.info[0], nullity = S.info[1];
+        alen = S.info[2];
         if (nullity == 0) {
             // appbas = x^(order-ord) * appbas, shift += order - ord
             const int k = order - ord;
@@ -465,41 +503,52 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             __syncthreads();
             break;
         }
-        if (rank == 0) continue;
-
-        // 5a. non-pivot rows += X * pivot rows (appbas d < alen, R ord < d < order)
-        const int nab = nullity * alen * cm;
-        const int nr = nullity * (order - ord - 1) * cn;
-        for (int idx = tid; idx < nab + nr; idx += nth) {
-            uint32_t *base;
-            int row, width, col, ia;
-            if (idx < nab) {
-                ia = idx / (alen * cm);
-                const int rem = idx - ia * alen * cm, d = rem / cm;
-                col = rem - d * cm;
-                width = ncm;
-                base = AB + (size_t)d * m * ncm;
-            } else {
-                const int j2 = idx - nab;
-                ia = j2 / ((order - ord - 1) * cn);
-                const int rem = j2 - ia * (order - ord - 1) * cn, d = ord + 1 + rem / cn;
-                col = rem % cn;
-                width = ncn;
-                base = R + (size_t)d * m * ncn;
-            }
-            row = S.nprow[ia];
-            uint64_t acc = base[row * width + col];
-            int b = 0;
-            for (; b + 8 <= rank; b += 8) {
-#pragma unroll
-                for (int u = 0; u < 8; u++) acc += (uint64_t)S.X[ia][b + u] * base[S.pivrow[b + u] * width + col];
-                acc = fold(acc, a.r32);
-            }
-            for (; b < rank; b++) acc += (uint64_t)S.X[ia][b] * base[S.pivrow[b] * width + col];
-            base[row * width + col] = mod64_q(acc, p, a.r32, a.r32q, a.oneq);
+        if (rank == 0) {
+            if (tid == 0) growf0[c] = 0;
+            continue;
         }
-        __syncthreads();
-        // 5b. pivot rows times x; length bound grows by one
+
+        // 5a. non-pivot rows += X * pivot rows: one (row, coefficient) slice per item,
+        //     appbas coefficients d < alen, R coefficients ord < d < order
+        const int nab = nullity * alen;
+        const int nr = nullity * (order - ord - 1);
+        int grow = 0;
+        for (int idx = tid; idx < nab + nr; idx += nth) {
+            const bool isab = idx < nab;
+            const int j2 = isab ? idx : idx - nab;
+            const int per = isab ? alen : (order - ord - 1);
+            const int ia = j2 / per;
+            const int d = isab ? j2 - ia * per : ord + 1 + (j2 - ia * per);
+            const int width = isab ? ncm : ncn, cols = isab ? cm : cn;
+            uint32_t *base = isab ? AB + (size_t)d * m * ncm : R + (size_t)d * m * ncn;
+            uint32_t *dst = base + S.nprow[ia] * width;
+            uint64_t acc[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] = (u < cols) ? dst[u] : 0ull;
+            for (int b0 = 0; b0 < rank; b0 += 8) {
+                const int bend = b0 + 8 < rank ? b0 + 8 : rank;
+                for (int b = b0; b < bend; b++) {
+                    const uint64_t xv = S.X[ia][b];
+                    const uint32_t *src = base + S.pivrow[b] * width;
+#pragma unroll
+                    for (int u = 0; u < 8; u++)
+                        if (u < cols) acc[u] += xv * src[u];
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++)
+                if (u < cols) dst[u] = mod64_q(acc[u], p, a.r32, a.r32q, a.oneq);
+        }
+        // growth test on this CTA's columns: a pivot row nonzero at coefficient alen-1
+        for (int idx = tid; idx < rank * cm; idx += nth) {
+            const int b = idx / cm, col = idx - b * cm;
+            if (AB[(size_t)(alen - 1) * m * ncm + S.pivrow[b] * ncm + col] != 0) grow = 1;
+        }
+        grow = __syncthreads_or(grow);
+        if (tid == 0) growf0[c] = grow;
+        // 5b. pivot rows times x (one coefficient more than the length: it may grow)
         const int nlen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
         for (int idx = tid; idx < rank * (cm + cn); idx += nth) {
             const int b = idx / (cm + cn), col = idx - b * (cm + cn);
@@ -515,15 +564,15 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             }
         }
         if (tid < rank) S.sh[S.pivrow[tid]] += 1;
-        alen = nlen;
         __syncthreads();
     }
 
-    // output: columns of this CTA, entry-major, zero beyond the length bound
+    // output: columns of this CTA, entry-major; coefficients past the length are zero
+    const int olen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
     for (int64_t idx = tid; idx < (int64_t)m * cm * a.ldo; idx += nth) {
         const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
         const int i = (int)(e / cm), il = (int)(e - (int64_t)i * cm);
-        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < alen ? (uint64_t)AB[(size_t)d * m * ncm + i * ncm + il] : 0ull;
+        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < olen ? (uint64_t)AB[(size_t)d * m * ncm + i * ncm + il] : 0ull;
     }
     if (c == 0 && tid < m) a.shift[tid] = S.sh[tid];
     cluster.sync();   // no CTA leaves while another may still address its shared memory
@@ -595,6 +644,7 @@ static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, i
         uint32_t inv = a.p;                       // Newton iteration for p^{-1} mod 2^32 (p odd)
         for (int i = 0; i < 5; i++) inv *= 2u - a.p * inv;
         a.pneg = 0u - inv;
+        a.r2 = (uint32_t)h_mulmod(a.r32, a.r32, a.p);
     }
     pmlg_ctx *ctx = S.ctx;
     const bool cluster = (a.p & 1u) && S.m <= LC_MAXM && S.n <= LC_MAXN && order <= LC_MAXORD;

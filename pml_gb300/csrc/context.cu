@@ -323,6 +323,10 @@ PMLG_API int pmlg_ctx_create(pmlg_ctx **out, int device)
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess) { delete ctx; return PMLG_ECUDA; }
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (cudaMalloc(&ctx->d_err, sizeof(int)) != cudaSuccess || cudaMemset(ctx->d_err, 0, sizeof(int)) != cudaSuccess) {
+        delete ctx;
+        return PMLG_ENOMEM;
+    }
     *out = ctx;
     return PMLG_OK;
 }
@@ -336,6 +340,7 @@ PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
     if (ctx->ws.ptr) cudaFree(ctx->ws.ptr);
     if (ctx->ws_aux.ptr) cudaFree(ctx->ws_aux.ptr);
     if (ctx->ws_pm.ptr) cudaFree(ctx->ws_pm.ptr);
+    if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     for (auto &r : ctx->prof) { cudaEventDestroy(r.beg); cudaEventDestroy(r.end); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
@@ -345,7 +350,7 @@ PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
 
 PMLG_API int pmlg_ctx_set_form(pmlg_ctx *ctx, int form)
 {
-    if (!ctx || form < PMLG_FORM_AUTO || form > PMLG_FORM_INT8_TC) return PMLG_EINVAL;
+    if (!ctx || form < PMLG_FORM_AUTO || form > PMLG_FORM_F16_TC) return PMLG_EINVAL;
     ctx->form = form;
     return PMLG_OK;
 }

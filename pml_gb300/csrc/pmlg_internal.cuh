@@ -129,6 +129,7 @@ struct pmlg_ctx
     void *pinned = nullptr;        // pinned staging for host-buffer entry points
     size_t pinned_bytes = 0;
     unsigned long long launches = 0;   // kernels launched through this context
+    int *d_err = nullptr;              // device error word: a bounded wait gave up
     // cached NTT tables
     static constexpr int kMaxTables = 64;
     pmlg::NttTable tables[kMaxTables];

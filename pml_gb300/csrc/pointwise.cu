@@ -13,6 +13,8 @@
 //    (tcgen05 kind::i8 does not exist on sm_103a; mma.sync is the INT8 path.)
 #include "pointwise.cuh"
 
+#include <cuda_fp16.h>
+
 namespace pmlg {
 
 constexpr int PW_PPC = 2;        // evaluation points per CTA
@@ -334,6 +336,263 @@ pw_cc2_kernel(PwArgs a)
 }
 
 // ---------------------------------------------------------------------------
+// FP16-digit tensor-core form (tcgen05, sm_103a)
+// ---------------------------------------------------------------------------
+//
+// Residues are centred (|x| < q/2 < 2^29) and written in balanced digits:
+//   A entries: 4 digits base 2^8,  |d_i| <= 128 ;  B entries: 3 digits base 2^10, |e_j| <= 512.
+// All digits are exact in FP16, every product d_i e_j is at most 2^16 in size,
+// and a sum over the 64 inner indices at most 2^22, so the FP32 accumulation
+// of the tensor cores is exact at every step (integers below 2^24).
+// Per point, two tcgen05.mma chains (M = 128, N = 192, K = 4 x 16) compute
+//   D0 = [A_0; A_1] [B_0 | B_1 | B_2]   and   D1 = [A_2; A_3] [B_0 | B_1 | B_2]
+// into TMEM (columns [0,192) and [256,448)), i.e. all 12 digit products
+// S_ij = A_i B_j.  The epilogue reads them back (tcgen05.ld), recombines
+//   C = sum_ij S_ij * 2^(8i + 10j)  mod q
+// on the CUDA cores (signed sums made non-negative with a multiple of q), and
+// adds the two TMEM lane halves (digits i and i+1 live 64 lanes apart).
+// Operands are staged in shared memory in the canonical no-swizzle K-major
+// layout (8 x 16-byte core matrices); two stages let the digit split of the
+// next point overlap the MMAs of the current one.  One CTA per SM walks over
+// the points; completion of each MMA chain is signalled on an mbarrier whose
+// wait is bounded (on time-out the kernel records an error and stops).
+
+constexpr int F16_THREADS = 256;
+constexpr int F16_A_BYTES = 128 * 64 * 2;           // one M=128 x K=64 FP16 operand
+constexpr int F16_B_BYTES = 192 * 64 * 2;           // N=192 x K=64
+constexpr int F16_STAGE = 2 * F16_A_BYTES + F16_B_BYTES;
+constexpr int F16_P_BYTES = 64 * 64 * 4;            // lane-half exchange buffer
+constexpr int F16_SMEM = 2 * F16_STAGE + F16_P_BYTES + 1024;   // + alignment slack
+constexpr uint32_t F16_TMEM_COLS = 512;
+constexpr long long F16_WAIT_LIMIT = 1ll << 20;   // try_wait polls; an MMA chain takes about a microsecond
+
+__device__ __forceinline__ uint32_t canon_off(int row, int k)
+{
+    // byte offset of (row, k) in a K-major no-swizzle tile with K = 64 (2-byte elements)
+    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
+{
+    // start address, LBO = 128 B (next core matrix along K), SBO = 1024 B (next 8 rows),
+    // descriptor version 1, no swizzle
+    return (uint64_t)((saddr >> 4) & 0x3fff) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ uint32_t pack_h2(int lo, int hi)
+{
+    const __half2 h = __halves2half2(__int2half_rn(lo), __int2half_rn(hi));
+    return *reinterpret_cast<const uint32_t *>(&h);
+}
+
+__device__ __forceinline__ void digits4(uint32_t x, uint32_t q, int (&d)[4])
+{
+    int t = (int)(x > (q >> 1) ? x - q : x);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int di = ((t + 128) & 255) - 128;
+        d[i] = di;
+        t = (t - di) >> 8;
+    }
+    d[3] = t;
+}
+
+__device__ __forceinline__ void digits3(uint32_t x, uint32_t q, int (&e)[3])
+{
+    int t = (int)(x > (q >> 1) ? x - q : x);
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const int ej = ((t + 512) & 1023) - 512;
+        e[j] = ej;
+        t = (t - ej) >> 10;
+    }
+    e[2] = t;
+}
+
+#define TC_LD16(taddr, v)                                                                                       \
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];" \
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),     \
+                   "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]) \
+                 : "r"(taddr))
+
+__global__ void __launch_bounds__(F16_THREADS, 1)
+pw_f16_kernel(PwArgs a)
+{
+    extern __shared__ unsigned char f16_raw[];
+    unsigned char *sm = (unsigned char *)(((uintptr_t)f16_raw + 1023) & ~(uintptr_t)1023);
+    uint32_t *P = (uint32_t *)(sm + 2 * F16_STAGE);
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int lg = ilog2_small(a.pt_tile);
+    const uint32_t q = a.q;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"((uint32_t)__cvta_generic_to_shared(&tmem_slot)), "r"(F16_TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+        s_abort = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
+
+    // digit split of one point into a stage (all threads); one warp writes one
+    // 8 x 8 core matrix (8 rows x 4 column pairs) per iteration: conflict-free
+    auto split = [&](int64_t pt, int stage) {
+        unsigned char *A01 = sm + stage * F16_STAGE;
+        unsigned char *A23 = A01 + F16_A_BYTES;
+        unsigned char *Bc = A23 + F16_A_BYTES;
+        const int row_in = lane >> 2, kp = lane & 3;
+        for (int cmi = warp; cmi < 64; cmi += F16_THREADS / 32) {
+            const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
+            uint32_t x0 = 0, x1 = 0;
+            if (i < a.r && l < a.k) x0 = a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)];
+            if (i < a.r && l + 1 < a.k) x1 = a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l + 1, lg, a.A.s_tile, a.s_e, a.s_p)];
+            int d0[4], d1[4];
+            digits4(x0, q, d0);
+            digits4(x1, q, d1);
+            const uint32_t o0 = canon_off(i, l), o1 = canon_off(64 + i, l);
+            *reinterpret_cast<uint32_t *>(A01 + o0) = pack_h2(d0[0], d1[0]);
+            *reinterpret_cast<uint32_t *>(A01 + o1) = pack_h2(d0[1], d1[1]);
+            *reinterpret_cast<uint32_t *>(A23 + o0) = pack_h2(d0[2], d1[2]);
+            *reinterpret_cast<uint32_t *>(A23 + o1) = pack_h2(d0[3], d1[3]);
+        }
+        for (int cmi = warp; cmi < 64; cmi += F16_THREADS / 32) {
+            // B operand row n (output column), K index l (inner index)
+            const int n = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
+            uint32_t y0 = 0, y1 = 0;
+            if (n < a.c && l < a.k) y0 = a.B.base[pw_off(pt, (int64_t)l * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)];
+            if (n < a.c && l + 1 < a.k) y1 = a.B.base[pw_off(pt, (int64_t)(l + 1) * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)];
+            int e0[3], e1[3];
+            digits3(y0, q, e0);
+            digits3(y1, q, e1);
+#pragma unroll
+            for (int j = 0; j < 3; j++)
+                *reinterpret_cast<uint32_t *>(Bc + canon_off(64 * j + n, l)) = pack_h2(e0[j], e1[j]);
+        }
+    };
+
+    auto issue = [&](int stage) {
+        // one thread: the 2 x 4 MMAs of a point, then a commit to the mbarrier
+        const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm + stage * F16_STAGE);
+        const uint32_t idesc = (1u << 4) | ((uint32_t)(192 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+#pragma unroll
+        for (int s = 0; s < 2; s++)
+#pragma unroll
+            for (int ks = 0; ks < 4; ks++) {
+                const uint64_t da = umma_desc(base + s * F16_A_BYTES + ks * 256);
+                const uint64_t db = umma_desc(base + 2 * F16_A_BYTES + ks * 256);
+                const uint32_t acc = ks > 0;
+                asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                             ::"r"(tmem + (uint32_t)(s * 256)), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            }
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
+                     : "memory");
+    };
+
+    const int64_t stride = gridDim.x;
+    int64_t pt = blockIdx.x;
+    int it = 0;
+    if (pt < a.npts) {
+        split(pt, 0);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (tid == 0) issue(0);
+    }
+    for (; pt < a.npts; pt += stride, it++) {
+        const int64_t nxt = pt + stride;
+        if (nxt < a.npts) {
+            split(nxt, (it + 1) & 1);
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        }
+        // wait for this point's MMAs (bounded)
+        {
+            uint32_t done = 0;
+            for (long long w = 0; w < F16_WAIT_LIMIT && !done; w++)
+                asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                             : "=r"(done) : "r"(mbar_addr), "r"((uint32_t)(it & 1)) : "memory");
+            if (!done) s_abort = 1;
+        }
+        __syncthreads();
+        if (s_abort) {
+            if (tid == 0 && a.err) atomicExch(a.err, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        // epilogue: warp w reads TMEM lanes 32 (w & 3) + lane, output columns [32 (w >> 2), +32)
+        {
+            const int L = 32 * (warp & 3) + lane;            // TMEM lane
+            const int i = L & 63, hi = L >> 6;                 // output row, digit parity
+            const int n0 = 32 * (warp >> 2);
+            const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int nb = n0 + 16 * h;
+                int64_t acc[16];
+#pragma unroll
+                for (int u = 0; u < 16; u++) acc[u] = 0;
+#pragma unroll
+                for (int j = 0; j < 3; j++) {
+                    uint32_t v0[16], v1[16];
+                    TC_LD16(lane_base + (uint32_t)(64 * j + nb), v0);
+                    TC_LD16(lane_base + (uint32_t)(256 + 64 * j + nb), v1);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    const int64_t w0 = a.wd[hi][j], w1 = a.wd[2 + hi][j];
+#pragma unroll
+                    for (int u = 0; u < 16; u++)
+                        acc[u] += (int64_t)__float2int_rn(__uint_as_float(v0[u])) * w0 +
+                                  (int64_t)__float2int_rn(__uint_as_float(v1[u])) * w1;
+                }
+                uint32_t r16[16];
+#pragma unroll
+                for (int u = 0; u < 16; u++)
+                    r16[u] = mod64_q((uint64_t)(acc[u] + (int64_t)a.negoff), q, a.r32, a.r32q, a.oneq);
+                // lanes 64..127 (odd digits) hand their partial sums to lanes 0..63
+                if (hi) {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) P[i * 64 + nb + u] = r16[u];
+                }
+                __syncthreads();
+                if (!hi && i < a.r) {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const int jcol = nb + u;
+                        if (jcol >= a.c) continue;
+                        uint32_t res = r16[u] + P[i * 64 + jcol];
+                        res = res >= q ? res - q : res;
+                        const int64_t off = pw_off(pt, (int64_t)i * a.ldc + jcol, lg, a.s_tile_c, a.s_e, a.s_p);
+                        if (a.accumulate) {
+                            res += a.C[off];
+                            res = res >= q ? res - q : res;
+                        }
+                        a.C[off] = res;
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (nxt < a.npts && tid == 0) issue((it + 1) & 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(F16_TMEM_COLS));
+}
+
+// ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
 
@@ -348,6 +607,9 @@ void pointwise_set_modulus(PwArgs &a, uint32_t q)
         a.w8[s] = (uint32_t)(w % q);
         w = (w << 8) % q;
     }
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 3; j++) a.wd[i][j] = (uint32_t)h_powmod(2, (uint64_t)(8 * i + 10 * j), q);
+    a.negoff = ((1ull << 56) / q + 1) * q;
 }
 
 static int form_resolve(int form)
@@ -363,14 +625,22 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
     if (!attr_done) {
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_i8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i8));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc2));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
         attr_done = true;
     }
     if (a.npts <= 0) return PMLG_OK;
     const int64_t grid = (a.npts + PW_PPC - 1) / PW_PPC;
     if (grid > 0x7fffffffll) return PMLG_EUNSUP;
-    if (form_resolve(form) == PMLG_FORM_INT8_TC) {
+    const int f = form_resolve(form);
+    if (f == PMLG_FORM_INT8_TC) {
         prof_begin(ctx, "pointwise_int8_tc", st);
         pw_i8_kernel<<<(unsigned)grid, PW_THREADS, smem_i8, st>>>(a);
+    } else if (f == PMLG_FORM_F16_TC) {
+        PwArgs b = a;
+        b.err = ctx->d_err;
+        const int64_t g3 = a.npts < ctx->sm_count ? a.npts : ctx->sm_count;
+        prof_begin(ctx, "pointwise_f16_tc", st);
+        pw_f16_kernel<<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
     } else {
         const int64_t items = (a.npts + 1) / 2;
         const int64_t g2 = items < ctx->sm_count ? items : ctx->sm_count;

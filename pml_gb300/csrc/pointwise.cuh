@@ -27,7 +27,10 @@ struct PwArgs
     int r, k, c;        // block shape, each <= 64
     uint32_t q, r32, r32q, oneq;
     uint32_t w8[7];     // 2^(8s) mod q for the limb recombination
+    uint32_t wd[4][3];  // 2^(8i + 10j) mod q for the FP16-digit recombination
+    uint64_t negoff;    // multiple of q >= 2^56, makes signed digit sums non-negative
     int accumulate;     // C += A*B instead of C = A*B
+    int *err;           // device error word (bounded waits that gave up), may be null
 };
 
 // Launches the chosen form over all points; blocks larger than 64 are split

@@ -34,7 +34,7 @@ def test_pmbasis_golden(ctx, case, leaf):
     assert np.array_equal(ab, as_u64(case["appbas"]))
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 @pytest.mark.parametrize("dims", [(4, 2, 64, 64), (6, 3, 100, 80), (8, 4, 129, 129), (16, 8, 256, 256),
                                   (5, 7, 40, 40), (1, 1, 30, 30), (10, 1, 50, 20)])
 def test_pmbasis_random(ctx, dims, form):

@@ -12,7 +12,7 @@ from conftest import P998, as_u64, golden, pm_from_seed, to_dev, to_host, vec_fr
 
 pytestmark = pytest.mark.gpu
 
-FORMS = [1, 2]   # PMLG_FORM_CUDA_CORE, PMLG_FORM_INT8_TC
+FORMS = [1, 2, 3]   # PMLG_FORM_CUDA_CORE, PMLG_FORM_INT8_TC, PMLG_FORM_F16_TC
 
 
 def _torch():
@@ -20,7 +20,7 @@ def _torch():
     return torch
 
 
-@pytest.fixture(params=FORMS, ids=["cuda_core", "int8_tc"])
+@pytest.fixture(params=FORMS, ids=["cuda_core", "int8_tc", "f16_tc"])
 def fctx(request, ctx):
     ctx.set_form(request.param)
     yield ctx
@@ -75,8 +75,11 @@ def test_batch_matmul_full_size_worst_case(ctx):
     C1 = _batch(ctx, A, B, p)
     ctx.set_form(2)
     C2 = _batch(ctx, A, B, p)
+    ctx.set_form(3)
+    C3 = _batch(ctx, A, B, p)
     ctx.set_form(0)
     assert np.array_equal(C1, C2)
+    assert np.array_equal(C1, C3)
     idx = [0, 1, 1234, 4095]
     assert np.array_equal(C1[idx], oracle.nmod_mat_mul_batch_u32(A[idx], B[idx], p))
 
@@ -160,9 +163,12 @@ def test_products_full_size_property(ctx):
     C1 = to_host(pml_gb300.nmod_poly_mat_multiply(dA, dB, p, ctx=ctx))
     ctx.set_form(2)
     C2 = to_host(pml_gb300.nmod_poly_mat_multiply(dA, dB, p, ctx=ctx))
+    ctx.set_form(3)
+    C3 = to_host(pml_gb300.nmod_poly_mat_multiply(dA, dB, p, ctx=ctx))
     ctx.set_form(0)
     torch.cuda.synchronize()
     assert np.array_equal(C1, C2)
+    assert np.array_equal(C1, C3)
     rng = np.random.default_rng(5)
     for _ in range(2):
         a = np.uint64(int(rng.integers(1, p)))
