@@ -19,17 +19,6 @@ namespace pmlg {
 
 __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 
-// Index of register slot (u, m) for a thread t in a group whose sub-transforms
-// have 2^G elements spaced 2^lls apart inside blocks of `span`.
-__device__ __forceinline__ int grp_index(int t, int u, int m, int G, int lls, int span)
-{
-    const int sub = 16 >> G;
-    const int sp = t * sub + u;
-    const int blk = sp >> lls;
-    const int off = sp & ((1 << lls) - 1);
-    return blk * span + off + (m << lls);
-}
-
 __device__ __forceinline__ uint32_t csub(uint32_t x, uint32_t m) { return min(x, x - m); }
 
 // Radix-2^G decimation-in-frequency butterflies on each of the 16 >> G
@@ -97,27 +86,115 @@ __device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &
     }
 }
 
-__device__ __forceinline__ void regs_to_smem(uint32_t *x, const uint32_t (&v)[16], int t, int G, int lls, int span)
-{
-#pragma unroll
-    for (int s = 0; s < 16; s++) x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))] = v[s];
-}
-
-__device__ __forceinline__ void smem_to_regs(uint32_t (&v)[16], const uint32_t *x, int t, int G, int lls, int span)
-{
-#pragma unroll
-    for (int s = 0; s < 16; s++) v[s] = x[sidx(grp_index(t, s >> G, s & ((1 << G) - 1), G, lls, span))];
-}
-
+// ---------------------------------------------------------------------------
+// Kernels, one instantiation per transform size 2^LG: every group's shape is a
+// compile-time constant, so the shared-memory exchange is one base address per
+// thread plus immediate offsets.  With the padding sidx(i) = i + i/16, the
+// padded index of slot s is sidx(base(t)) + sidx(c_s), because c_s is either
+// a multiple of 16 or cannot carry the base across a multiple of 16.
 // ---------------------------------------------------------------------------
 
+template <int LG, int GI>
+struct FwdGeom
+{
+    static constexpr int NG = (LG + 3) / 4;
+    static constexpr int G = (GI < NG - 1) ? 4 : LG - 4 * (NG - 1);
+    static constexpr int LGH = LG - 1 - 4 * GI;        // log2 of the group's top half size
+    static constexpr int LLS = LGH - (G - 1);          // log2 of the sub-transform spacing
+    static constexpr int SPAN = 2 << LGH;
+};
+
+template <int LG, int GI>
+struct InvGeom
+{
+    static constexpr int NG = (LG + 3) / 4;
+    static constexpr int GFIRST = LG - 4 * (NG - 1);
+    static constexpr int G = GI == 0 ? GFIRST : 4;
+    static constexpr int LLS = GI == 0 ? 0 : GFIRST + 4 * (GI - 1);
+    static constexpr int SPAN = 1 << (LLS + G);
+};
+
+// padded shared-memory index of slot 0 of thread t in a group (G, LLS, SPAN)
+template <int G, int LLS, int SPAN>
+__device__ __forceinline__ int grp_pbase(int t)
+{
+    if constexpr (G == 4) {
+        const int base = (t >> LLS) * SPAN + (t & ((1 << LLS) - 1));
+        return base + (base >> 4);
+    } else {
+        return 17 * t;   // 16 consecutive residues per thread
+    }
+}
+
+// padded offset of slot s relative to grp_pbase
+template <int G, int LLS>
+__device__ __forceinline__ constexpr int grp_poff(int s)
+{
+    return G == 4 ? (s << LLS) + ((s << LLS) >> 4) : s;
+}
+
+template <int G, int LLS, int SPAN>
+__device__ __forceinline__ void regs_to_smem_t(uint32_t *x, const uint32_t (&v)[16], int t)
+{
+    uint32_t *p = x + grp_pbase<G, LLS, SPAN>(t);
+#pragma unroll
+    for (int s = 0; s < 16; s++) p[grp_poff<G, LLS>(s)] = v[s];
+}
+
+template <int G, int LLS, int SPAN>
+__device__ __forceinline__ void smem_to_regs_t(uint32_t (&v)[16], const uint32_t *x, int t)
+{
+    const uint32_t *p = x + grp_pbase<G, LLS, SPAN>(t);
+#pragma unroll
+    for (int s = 0; s < 16; s++) v[s] = p[grp_poff<G, LLS>(s)];
+}
+
+template <int LG, int GI>
+__device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
+{
+    if constexpr (GI < FwdGeom<LG, 0>::NG) {
+        using Gm = FwdGeom<LG, GI>;
+        if constexpr (GI > 0) {
+            __syncthreads();
+            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
+        }
+        dif_const<Gm::G>(v, T);
+        if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
+        if constexpr (GI < Gm::NG - 1) {
+            __syncthreads();   // everyone done reading the previous layout
+            regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
+        }
+        fwd_groups<LG, GI + 1>(v, x, t, T);
+    }
+}
+
+template <int LG, int GI>
+__device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
+{
+    if constexpr (GI < InvGeom<LG, 0>::NG) {
+        using Gm = InvGeom<LG, GI>;
+        if constexpr (GI > 0) {
+            __syncthreads();
+            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
+        }
+        if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
+        dit_const<Gm::G>(v, T);
+        if constexpr (GI < Gm::NG - 1) {
+            __syncthreads();
+            regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
+        }
+        inv_groups<LG, GI + 1>(v, x, t, T);
+    }
+}
+
+template <int LG>
 __global__ void __launch_bounds__(1024)
 ntt_fwd_kernel(NttFwdArgs a)
 {
     extern __shared__ uint32_t smem[];
-    const int lg = a.lg, N = 1 << lg, TPT = N >> 4;
-    const int tpc = blockDim.x >> (lg - 4);
-    const int sub = threadIdx.x >> (lg - 4), t = threadIdx.x & (TPT - 1);
+    constexpr int N = 1 << LG, TPT = N >> 4;
+    const int tpc = blockDim.x / TPT;
+    const int sub = threadIdx.x / TPT, t = threadIdx.x % TPT;
     const int64_t e = (int64_t)blockIdx.x * tpc + sub;
     const int j = blockIdx.y;
     const NttDev &T = a.tab[j];
@@ -140,31 +217,7 @@ ntt_fwd_kernel(NttFwdArgs a)
             v[m] = val;
         }
     }
-    const int ngroups = (lg + 3) >> 2;
-    int lgH = lg - 1;
-    for (int gi = 0; gi < ngroups; gi++) {
-        const int G = (gi < ngroups - 1) ? 4 : lg - 4 * (ngroups - 1);
-        const int lls = lgH - (G - 1), span = 2 << lgH;
-        if (gi > 0) {
-            __syncthreads();
-            smem_to_regs(v, x, t, G, lls, span);
-        }
-        if (G == 4) {
-            dif_const<4>(v, T);
-            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls);
-        } else if (G == 3) {
-            dif_const<3>(v, T);
-        } else if (G == 2) {
-            dif_const<2>(v, T);
-        } else {
-            dif_const<1>(v, T);
-        }
-        if (gi < ngroups - 1) {
-            __syncthreads();   // everyone done reading the previous layout
-            regs_to_smem(x, v, t, G, lls, span);
-        }
-        lgH -= G;
-    }
+    fwd_groups<LG, 0>(v, x, t, T);
     // the last group leaves points 16t .. 16t+15 in v[0..15]
     if (active) {
         uint32_t *dst = a.out + j * a.prime_stride + e * kPtTile;
@@ -179,13 +232,14 @@ ntt_fwd_kernel(NttFwdArgs a)
     }
 }
 
+template <int LG>
 __global__ void __launch_bounds__(1024)
 ntt_inv_kernel(NttInvArgs a)
 {
     extern __shared__ uint32_t smem[];
-    const int lg = a.lg, N = 1 << lg, TPT = N >> 4;
-    const int tpc = blockDim.x >> (lg - 4);
-    const int sub = threadIdx.x >> (lg - 4), t = threadIdx.x & (TPT - 1);
+    constexpr int N = 1 << LG, TPT = N >> 4;
+    const int tpc = blockDim.x / TPT;
+    const int sub = threadIdx.x / TPT, t = threadIdx.x % TPT;
     const int64_t e = (int64_t)blockIdx.x * tpc + sub;
     const int j = blockIdx.y;
     const NttDev &T = a.tab[j];
@@ -204,32 +258,7 @@ ntt_inv_kernel(NttInvArgs a)
 #pragma unroll
         for (int m = 0; m < 16; m++) v[m] = 0;
     }
-    const int ngroups = (lg + 3) >> 2;
-    const int Gfirst = lg - 4 * (ngroups - 1);
-    int lls = 0;
-    for (int gi = 0; gi < ngroups; gi++) {
-        const int G = (gi == 0) ? Gfirst : 4;
-        const int span = 1 << (lls + G);
-        if (gi > 0) {
-            __syncthreads();
-            smem_to_regs(v, x, t, G, lls, span);
-        }
-        if (G == 4) {
-            if (lls > 0) group_twiddles(v, T, t & ((1 << lls) - 1), lls);
-            dit_const<4>(v, T);
-        } else if (G == 3) {
-            dit_const<3>(v, T);
-        } else if (G == 2) {
-            dit_const<2>(v, T);
-        } else {
-            dit_const<1>(v, T);
-        }
-        if (gi < ngroups - 1) {
-            __syncthreads();
-            regs_to_smem(x, v, t, G, lls, span);
-        }
-        lls += G;
-    }
+    inv_groups<LG, 0>(v, x, t, T);
     // last group: element m of thread t is coefficient t + m * N/16
     if (!active) return;
 #pragma unroll
@@ -297,16 +326,41 @@ static void ntt_geometry(int lg, int64_t nent, int *threads, int *tpc, size_t *s
     *blocks = (nent + *tpc - 1) / *tpc;
 }
 
+template <int LG>
+static cudaError_t set_attrs()
+{
+    const int sm = (int)(((1 << LG) + (1 << (LG - 4))) * sizeof(uint32_t) * ((1 << (LG - 4)) >= 256 ? 1 : 256 >> (LG - 4)));
+    cudaError_t e = cudaFuncSetAttribute(ntt_fwd_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(ntt_inv_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    return e;
+}
+
 static int ensure_smem_attr(pmlg_ctx *ctx)
 {
     static bool done = false;
     if (done) return PMLG_OK;
-    const int maxsm = (int)(((1 << kMaxLgN) + (1 << (kMaxLgN - 4))) * sizeof(uint32_t)) * 1;
-    PMLG_CUDA_TRY(cudaFuncSetAttribute(ntt_fwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm + 4096));
-    PMLG_CUDA_TRY(cudaFuncSetAttribute(ntt_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, maxsm + 4096));
+    PMLG_CUDA_TRY(set_attrs<4>());  PMLG_CUDA_TRY(set_attrs<5>());  PMLG_CUDA_TRY(set_attrs<6>());
+    PMLG_CUDA_TRY(set_attrs<7>());  PMLG_CUDA_TRY(set_attrs<8>());  PMLG_CUDA_TRY(set_attrs<9>());
+    PMLG_CUDA_TRY(set_attrs<10>()); PMLG_CUDA_TRY(set_attrs<11>()); PMLG_CUDA_TRY(set_attrs<12>());
+    PMLG_CUDA_TRY(set_attrs<13>()); PMLG_CUDA_TRY(set_attrs<14>());
     done = true;
     return PMLG_OK;
 }
+
+#define NTT_DISPATCH(KERNEL, LGV, GRID, TH, SMEM, ST, ARGS)                      \
+    switch (LGV) {                                                                \
+    case 4: KERNEL<4><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 5: KERNEL<5><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 6: KERNEL<6><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 7: KERNEL<7><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 8: KERNEL<8><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 9: KERNEL<9><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
+    case 10: KERNEL<10><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    case 11: KERNEL<11><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    case 12: KERNEL<12><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    case 13: KERNEL<13><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    default: KERNEL<14><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    }
 
 int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a, cudaStream_t st)
 {
@@ -319,7 +373,7 @@ int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a, cudaStream_t st)
     ntt_geometry(a.lg, a.nent, &threads, &tpc, &smem, &blocks);
     if (blocks > 0x7fffffffll) return PMLG_EUNSUP;
     prof_begin(ctx, "ntt_fwd", st);
-    ntt_fwd_kernel<<<dim3((unsigned)blocks, a.t), threads, smem, st>>>(a);
+    NTT_DISPATCH(ntt_fwd_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
@@ -337,7 +391,7 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st)
     ntt_geometry(a.lg, a.nent, &threads, &tpc, &smem, &blocks);
     if (blocks > 0x7fffffffll) return PMLG_EUNSUP;
     prof_begin(ctx, "ntt_inv", st);
-    ntt_inv_kernel<<<dim3((unsigned)blocks, a.t), threads, smem, st>>>(a);
+    NTT_DISPATCH(ntt_inv_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());

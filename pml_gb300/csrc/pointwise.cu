@@ -446,38 +446,44 @@ pw_f16_kernel(PwArgs a)
     const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
 
     // digit split of one point into a stage (all threads); one warp writes one
-    // 8 x 8 core matrix (8 rows x 4 column pairs) per iteration: conflict-free
+    // 8 x 8 core matrix (8 rows x 4 column pairs) per iteration: conflict-free.
+    // All 32 global loads of a lane are issued before any is used.
     auto split = [&](int64_t pt, int stage) {
         unsigned char *A01 = sm + stage * F16_STAGE;
         unsigned char *A23 = A01 + F16_A_BYTES;
         unsigned char *Bc = A23 + F16_A_BYTES;
         const int row_in = lane >> 2, kp = lane & 3;
-        for (int cmi = warp; cmi < 64; cmi += F16_THREADS / 32) {
+        constexpr int NIT = 64 / (F16_THREADS / 32);
+        uint32_t xa[NIT][2], yb[NIT][2];
+#pragma unroll
+        for (int itn = 0; itn < NIT; itn++) {
+            const int cmi = warp + itn * (F16_THREADS / 32);
             const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
-            uint32_t x0 = 0, x1 = 0;
-            if (i < a.r && l < a.k) x0 = a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)];
-            if (i < a.r && l + 1 < a.k) x1 = a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l + 1, lg, a.A.s_tile, a.s_e, a.s_p)];
+            xa[itn][0] = (i < a.r && l < a.k) ? a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)] : 0u;
+            xa[itn][1] = (i < a.r && l + 1 < a.k) ? a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l + 1, lg, a.A.s_tile, a.s_e, a.s_p)] : 0u;
+            // B operand row n (output column), K index l (inner index)
+            const int n = i;
+            yb[itn][0] = (n < a.c && l < a.k) ? a.B.base[pw_off(pt, (int64_t)l * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)] : 0u;
+            yb[itn][1] = (n < a.c && l + 1 < a.k) ? a.B.base[pw_off(pt, (int64_t)(l + 1) * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)] : 0u;
+        }
+#pragma unroll
+        for (int itn = 0; itn < NIT; itn++) {
+            const int cmi = warp + itn * (F16_THREADS / 32);
+            const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
             int d0[4], d1[4];
-            digits4(x0, q, d0);
-            digits4(x1, q, d1);
+            digits4(xa[itn][0], q, d0);
+            digits4(xa[itn][1], q, d1);
             const uint32_t o0 = canon_off(i, l), o1 = canon_off(64 + i, l);
             *reinterpret_cast<uint32_t *>(A01 + o0) = pack_h2(d0[0], d1[0]);
             *reinterpret_cast<uint32_t *>(A01 + o1) = pack_h2(d0[1], d1[1]);
             *reinterpret_cast<uint32_t *>(A23 + o0) = pack_h2(d0[2], d1[2]);
             *reinterpret_cast<uint32_t *>(A23 + o1) = pack_h2(d0[3], d1[3]);
-        }
-        for (int cmi = warp; cmi < 64; cmi += F16_THREADS / 32) {
-            // B operand row n (output column), K index l (inner index)
-            const int n = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
-            uint32_t y0 = 0, y1 = 0;
-            if (n < a.c && l < a.k) y0 = a.B.base[pw_off(pt, (int64_t)l * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)];
-            if (n < a.c && l + 1 < a.k) y1 = a.B.base[pw_off(pt, (int64_t)(l + 1) * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)];
             int e0[3], e1[3];
-            digits3(y0, q, e0);
-            digits3(y1, q, e1);
+            digits3(yb[itn][0], q, e0);
+            digits3(yb[itn][1], q, e1);
 #pragma unroll
             for (int j = 0; j < 3; j++)
-                *reinterpret_cast<uint32_t *>(Bc + canon_off(64 * j + n, l)) = pack_h2(e0[j], e1[j]);
+                *reinterpret_cast<uint32_t *>(Bc + canon_off(64 * j + i, l)) = pack_h2(e0[j], e1[j]);
         }
     };
 
