@@ -178,10 +178,28 @@ def cpu_product_ms(nthreads: int, reps: int, warm: int):
     return statistics.median(t), t
 
 
+def rank_barrier(world: int) -> None:
+    """Barrier across the replicas (no-op for one process)."""
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    """Slowest replica's time: the job is done when the last rank is."""
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
-        return
+        return   # the reference arm runs on rank 0 only; the other ranks exit without work
     nthreads = os.cpu_count() or 1
     med, ts = cpu_product_ms(nthreads, max(args.steps, 1), max(args.warmup, 0))
     line = {
@@ -244,15 +262,10 @@ def run_pml(args):
                                             R, K, C, LEN, LEN, P, st.cuda_stream))
 
     def barrier():
-        if world > 1:
-            torch.distributed.barrier()
+        rank_barrier(world)
 
-    def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+    def ranks_max(x: float) -> float:
+        return max_over_ranks(x, world, dev)
 
     def timed(form: int, steps: int, warmup: int, clocks=False):
         ctx.set_form(form)
@@ -276,7 +289,7 @@ def run_pml(args):
         if sampler:
             sampler.__exit__(None, None, None)
         ms = e0.elapsed_time(e1) / steps
-        return max_over_ranks(ms), ctx.launches - l0, (sampler.summary() if sampler else None)
+        return ranks_max(ms), ctx.launches - l0, (sampler.summary() if sampler else None)
 
     FORMS = (("f16_tc", pml_gb300.FORM_F16_TC), ("int8_tc", pml_gb300.FORM_INT8_TC),
              ("cuda_core", pml_gb300.FORM_CUDA_CORE))
@@ -361,7 +374,7 @@ def run_pml(args):
     e1.record(st)
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    e2e_ms = ranks_max(e0.elapsed_time(e1) / args.steps)
     e2e_ok = bool(torch.equal(hC, dC.cpu()))
     h2d = 2 * R * K * LEN * 8
     d2h = R * C * (2 * LEN - 1) * 8
@@ -381,7 +394,7 @@ def run_pml(args):
             t0 = time.perf_counter()
             ab, sh = pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
             torch.cuda.synchronize()
-            pm[name + "_ms"] = max_over_ranks((time.perf_counter() - t0) * 1e3)
+            pm[name + "_ms"] = ranks_max((time.perf_counter() - t0) * 1e3)
             outs[name] = (ab, sh)
         ctx.set_profiling(True)
         ctx.set_form(HEAD)
