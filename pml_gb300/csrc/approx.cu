@@ -350,19 +350,23 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     const int m0 = c * ncm, n0 = c * ncn;
     const int cm = m0 < m ? (m - m0 < ncm ? m - m0 : ncm) : 0;
     const int cn = n0 < n ? (n - n0 < ncn ? n - n0 : ncn) : 0;
-    uint32_t *AB = dyn;                                      // [order+1][m][ncm]
-    uint32_t *R = dyn + (size_t)(order + 1) * m * ncm;       // [order][m][ncn]
+    // coefficient d of the slices starts at d * sab (appbas) and d * sr (R): the
+    // strides are odd, so threads working on consecutive coefficients of the
+    // same row hit distinct banks
+    const int sab = m * ncm + 1, sr = m * ncn + 1;
+    uint32_t *AB = dyn;                                      // [order+1][m][ncm], padded
+    uint32_t *R = dyn + (size_t)(order + 1) * sab;           // [order][m][ncn], padded
     const int64_t fl = a.flen < order ? a.flen : order;
 
     for (int idx = tid; idx < order * m * ncn; idx += nth) {
         const int d = idx / (m * ncn), rem = idx - d * m * ncn, i = rem / ncn, jl = rem - i * ncn;
         uint32_t v = 0;
         if (jl < cn && d < fl) v = (uint32_t)a.F[((int64_t)i * n + n0 + jl) * a.ldF + d];
-        R[idx] = v;
+        R[(size_t)d * sr + rem] = v;
     }
     for (int idx = tid; idx < (order + 1) * m * ncm; idx += nth) {
         const int d = idx / (m * ncm), rem = idx - d * m * ncm, i = rem / ncm, il = rem - i * ncm;
-        AB[idx] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
+        AB[(size_t)d * sab + rem] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
     }
     if (tid < m) S.sh[tid] = a.shift[tid];
     if (tid < LC_CL) S.growf[tid] = 0;
@@ -390,7 +394,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         // 2. gather the permuted R[ord]^T into CTA 0
         for (int idx = tid; idx < m * cn; idx += nth) {
             const int r = idx / cn, jl = idx - r * cn;
-            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[((size_t)ord * m + S.perm[r]) * ncn + jl];
+            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[(size_t)ord * sr + S.perm[r] * ncn + jl];
         }
         cluster.sync();
 
@@ -495,8 +499,8 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             // appbas = x^(order-ord) * appbas, shift += order - ord
             const int k = order - ord;
             for (int idx = tid; idx < m * ncm; idx += nth) {
-                for (int d = alen - 1; d >= 0; d--) AB[((size_t)(d + k)) * m * ncm + idx] = AB[(size_t)d * m * ncm + idx];
-                for (int d = 0; d < k; d++) AB[(size_t)d * m * ncm + idx] = 0;
+                for (int d = alen - 1; d >= 0; d--) AB[((size_t)(d + k)) * sab + idx] = AB[(size_t)d * sab + idx];
+                for (int d = 0; d < k; d++) AB[(size_t)d * sab + idx] = 0;
             }
             if (tid < m) S.sh[tid] += k;
             alen += k;
@@ -520,7 +524,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             const int ia = j2 / per;
             const int d = isab ? j2 - ia * per : ord + 1 + (j2 - ia * per);
             const int width = isab ? ncm : ncn, cols = isab ? cm : cn;
-            uint32_t *base = isab ? AB + (size_t)d * m * ncm : R + (size_t)d * m * ncn;
+            uint32_t *base = isab ? AB + (size_t)d * sab : R + (size_t)d * sr;
             uint32_t *dst = base + S.nprow[ia] * width;
             uint64_t acc[8];
 #pragma unroll
@@ -544,7 +548,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         // growth test on this CTA's columns: a pivot row nonzero at coefficient alen-1
         for (int idx = tid; idx < rank * cm; idx += nth) {
             const int b = idx / cm, col = idx - b * cm;
-            if (AB[(size_t)(alen - 1) * m * ncm + S.pivrow[b] * ncm + col] != 0) grow = 1;
+            if (AB[(size_t)(alen - 1) * sab + S.pivrow[b] * ncm + col] != 0) grow = 1;
         }
         grow = __syncthreads_or(grow);
         if (tid == 0) growf0[c] = grow;
@@ -555,12 +559,12 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             const int row = S.pivrow[b];
             if (col < cm) {
                 for (int d = nlen - 1; d > 0; d--)
-                    AB[(size_t)d * m * ncm + row * ncm + col] = AB[(size_t)(d - 1) * m * ncm + row * ncm + col];
+                    AB[(size_t)d * sab + row * ncm + col] = AB[(size_t)(d - 1) * sab + row * ncm + col];
                 AB[row * ncm + col] = 0;
             } else {
                 const int j = col - cm;
                 for (int d = order - 1; d > ord; d--)
-                    R[(size_t)d * m * ncn + row * ncn + j] = R[(size_t)(d - 1) * m * ncn + row * ncn + j];
+                    R[(size_t)d * sr + row * ncn + j] = R[(size_t)(d - 1) * sr + row * ncn + j];
             }
         }
         if (tid < rank) S.sh[S.pivrow[tid]] += 1;
@@ -572,7 +576,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     for (int64_t idx = tid; idx < (int64_t)m * cm * a.ldo; idx += nth) {
         const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
         const int i = (int)(e / cm), il = (int)(e - (int64_t)i * cm);
-        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < olen ? (uint64_t)AB[(size_t)d * m * ncm + i * ncm + il] : 0ull;
+        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < olen ? (uint64_t)AB[(size_t)d * sab + i * ncm + il] : 0ull;
     }
     if (c == 0 && tid < m) a.shift[tid] = S.sh[tid];
     cluster.sync();   // no CTA leaves while another may still address its shared memory
@@ -581,7 +585,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
 static size_t leaf_cluster_smem(int m, int n, int order)
 {
     const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
-    return ((size_t)(order + 1) * m * ncm + (size_t)order * m * ncn) * sizeof(uint32_t);
+    return ((size_t)(order + 1) * (m * ncm + 1) + (size_t)order * (m * ncn + 1)) * sizeof(uint32_t);
 }
 
 // ---------------------------------------------------------------------------

@@ -336,35 +336,50 @@ pw_cc2_kernel(PwArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// FP16-digit tensor-core form (tcgen05, sm_103a)
+// FP16-digit tensor-core form (tcgen05.mma kind::f16, FP32 accumulators in TMEM)
 // ---------------------------------------------------------------------------
 //
 // Residues are centred (|x| < q/2 < 2^29) and written in balanced digits:
 //   A entries: 4 digits base 2^8,  |d_i| <= 128 ;  B entries: 3 digits base 2^10, |e_j| <= 512.
 // All digits are exact in FP16, every product d_i e_j is at most 2^16 in size,
 // and a sum over the 64 inner indices at most 2^22, so the FP32 accumulation
-// of the tensor cores is exact at every step (integers below 2^24).
-// Per point, two tcgen05.mma chains (M = 128, N = 192, K = 4 x 16) compute
-//   D0 = [A_0; A_1] [B_0 | B_1 | B_2]   and   D1 = [A_2; A_3] [B_0 | B_1 | B_2]
-// into TMEM (columns [0,192) and [256,448)), i.e. all 12 digit products
-// S_ij = A_i B_j.  The epilogue reads them back (tcgen05.ld), recombines
-//   C = sum_ij S_ij * 2^(8i + 10j)  mod q
-// on the CUDA cores (signed sums made non-negative with a multiple of q), and
-// adds the two TMEM lane halves (digits i and i+1 live 64 lanes apart).
-// Operands are staged in shared memory in the canonical no-swizzle K-major
-// layout (8 x 16-byte core matrices); two stages let the digit split of the
-// next point overlap the MMAs of the current one.  One CTA per SM walks over
-// the points; completion of each MMA chain is signalled on an mbarrier whose
-// wait is bounded (on time-out the kernel records an error and stops).
+// of the tensor cores is exact at every step (integers of at most 2^22).
+//
+// Per point the MMAs compute all 12 digit products S_ij = A_i B_j; the
+// epilogue recombines C = sum_ij S_ij 2^(8i + 10j) mod q on the CUDA cores.
+// The A operand is stacked two digits high (M = 128: rows 0..63 digit 2s,
+// rows 64..127 digit 2s+1, stack s = 0, 1), the B operand holds the three
+// digits side by side.  The output columns are split into two regions
+// (columns 0..31 and 32..63), each with its own TMEM range and mbarriers, so
+// the MMAs of the next point fill one region while the epilogue still reads
+// the other:  region h = 2 stacks x (N = 96 = 3 digits x 32 columns).
+//
+// The CTA is warp-specialised (one CTA per SM, points taken in pairs):
+//   warps 0..7   epilogue: tcgen05.ld, integer recombination, reduction mod q,
+//                staging in shared memory, coalesced write of the pair;
+//   warps 8..15  loads of a point pair (the two points share 8 bytes in the
+//                point-tiled layout) and the digit split into two stages;
+//   warp 16      one thread issues the MMAs and commits to the mbarriers.
+// Digits reach FP16 without conversion instructions: 0x6400 + u is the FP16
+// encoding of 1024 + u for 0 <= u <= 1024, and one packed subtraction removes
+// the bias.  The FP32 sums come back as integers the same way: for |S| <= 2^22
+// the encoding of S + 1.5 * 2^23 is 0x4B400000 + S.
+// Every mbarrier wait is bounded; a wait that gives up raises a shared abort
+// flag that turns every later wait into a no-op, so all warps leave their
+// loops, the MMAs in flight are drained and the kernel records the error.
 
-constexpr int F16_THREADS = 256;
-constexpr int F16_A_BYTES = 128 * 64 * 2;           // one M=128 x K=64 FP16 operand
-constexpr int F16_B_BYTES = 192 * 64 * 2;           // N=192 x K=64
+constexpr int F16_EPI_WARPS = 8;
+constexpr int F16_SPLIT_WARPS = 8;
+constexpr int F16_MMA_WARP = F16_EPI_WARPS + F16_SPLIT_WARPS;
+constexpr int F16_THREADS = (F16_MMA_WARP + 1) * 32;
+constexpr int F16_A_BYTES = 128 * 64 * 2;            // one stack: M = 128 x K = 64, FP16
+constexpr int F16_B_BYTES = 192 * 64 * 2;            // N = 2 regions x 96, K = 64
 constexpr int F16_STAGE = 2 * F16_A_BYTES + F16_B_BYTES;
-constexpr int F16_P_BYTES = 64 * 64 * 4;            // lane-half exchange buffer
-constexpr int F16_SMEM = 2 * F16_STAGE + F16_P_BYTES + 1024;   // + alignment slack
+constexpr int F16_CST_LD = 68;                       // padded staging row (words): conflict-free v4 stores
+constexpr int F16_CST_WORDS = 64 * F16_CST_LD;       // one (point, digit parity) plane
+constexpr int F16_SMEM = 2 * F16_STAGE + 4 * F16_CST_WORDS * 4 + 1024;   // + alignment slack
 constexpr uint32_t F16_TMEM_COLS = 512;
-constexpr long long F16_WAIT_LIMIT = 1ll << 20;   // try_wait polls; an MMA chain takes about a microsecond
+constexpr long long F16_WAIT_LIMIT = 1ll << 20;      // try_wait polls; a legitimate wait lasts microseconds
 
 __device__ __forceinline__ uint32_t canon_off(int row, int k)
 {
@@ -380,34 +395,71 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
            ((uint64_t)1 << 46);
 }
 
-__device__ __forceinline__ uint32_t pack_h2(int lo, int hi)
+__device__ __forceinline__ void mbar_init(uint64_t *b, uint32_t count)
 {
-    const __half2 h = __halves2half2(__int2half_rn(lo), __int2half_rn(hi));
-    return *reinterpret_cast<const uint32_t *>(&h);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"((uint32_t)__cvta_generic_to_shared(b)), "r"(count));
 }
 
-__device__ __forceinline__ void digits4(uint32_t x, uint32_t q, int (&d)[4])
+__device__ __forceinline__ void mbar_arrive(uint64_t *b)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(b)) : "memory");
+}
+
+// Bounded wait for the phase of the given parity; false when it gave up (or
+// another warp already did), in which case the abort flag is set.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort)
+{
+    const uint32_t addr = (uint32_t)__cvta_generic_to_shared(b);
+    for (long long w = 0; w < F16_WAIT_LIMIT; w++) {
+        uint32_t done;
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+        if (done) return true;
+        if (abort && *abort) return false;
+    }
+    if (abort) *abort = 1;
+    return false;
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t *b)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+                 ::"r"((uint32_t)__cvta_generic_to_shared(b)) : "memory");
+}
+
+// FP16 encodings 0x6400 + (d + 128) of the balanced base-2^8 digits d of x (centred mod q)
+__device__ __forceinline__ void digits4h(uint32_t x, uint32_t q, uint32_t (&h)[4])
 {
     int t = (int)(x > (q >> 1) ? x - q : x);
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        const int di = ((t + 128) & 255) - 128;
-        d[i] = di;
-        t = (t - di) >> 8;
+        const int tt = t + 128;
+        h[i] = (uint32_t)(tt & 255) + 0x6400u;
+        t = tt >> 8;
     }
-    d[3] = t;
+    h[3] = (uint32_t)(t + 128) + 0x6400u;
 }
 
-__device__ __forceinline__ void digits3(uint32_t x, uint32_t q, int (&e)[3])
+// FP16 encodings 0x6400 + (e + 512) of the balanced base-2^10 digits e of x (centred mod q);
+// the top digit lies in [-512, 512], so its encoding can reach 0x6800 (= 2048, still exact)
+__device__ __forceinline__ void digits3h(uint32_t x, uint32_t q, uint32_t (&h)[3])
 {
     int t = (int)(x > (q >> 1) ? x - q : x);
 #pragma unroll
     for (int j = 0; j < 2; j++) {
-        const int ej = ((t + 512) & 1023) - 512;
-        e[j] = ej;
-        t = (t - ej) >> 10;
+        const int tt = t + 512;
+        h[j] = (uint32_t)(tt & 1023) + 0x6400u;
+        t = tt >> 10;
     }
-    e[2] = t;
+    h[2] = (uint32_t)(t + 512) + 0x6400u;
+}
+
+// two biased FP16 encodings -> one half2 of the digit values
+__device__ __forceinline__ uint32_t unbias_pair(uint32_t h0, uint32_t h1, uint32_t bias2)
+{
+    uint32_t w = __byte_perm(h0, h1, 0x5410), r;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(w), "r"(bias2));
+    return r;
 }
 
 #define TC_LD16(taddr, v)                                                                                       \
@@ -416,18 +468,33 @@ __device__ __forceinline__ void digits3(uint32_t x, uint32_t q, int (&e)[3])
                    "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]) \
                  : "r"(taddr))
 
+// values of entry e at points pt0 and pt0 + 1
+template <bool TILE>
+__device__ __forceinline__ uint2 f16_load_pair(const PwOperand &op, int64_t e, int64_t pt0, bool has1, int lg,
+                                               const PwArgs &a)
+{
+    if (TILE)   // point-tiled layout, pt0 even: the two values are adjacent
+        return __ldg(reinterpret_cast<const uint2 *>(op.base + ((pt0 >> 2) * op.s_tile + e * 4 + (pt0 & 3))));
+    uint2 v;
+    v.x = op.base[pw_off(pt0, e, lg, op.s_tile, a.s_e, a.s_p)];
+    v.y = has1 ? op.base[pw_off(pt0 + 1, e, lg, op.s_tile, a.s_e, a.s_p)] : 0u;
+    return v;
+}
+
+template <bool TILE>
 __global__ void __launch_bounds__(F16_THREADS, 1)
 pw_f16_kernel(PwArgs a)
 {
     extern __shared__ unsigned char f16_raw[];
     unsigned char *sm = (unsigned char *)(((uintptr_t)f16_raw + 1023) & ~(uintptr_t)1023);
-    uint32_t *P = (uint32_t *)(sm + 2 * F16_STAGE);
-    __shared__ __align__(8) uint64_t mbar;
+    uint32_t *Cst = (uint32_t *)(sm + 2 * F16_STAGE);
+    __shared__ __align__(8) uint64_t full[2], empty[2], tfull[2], tempty[2], drain;
     __shared__ uint32_t tmem_slot;
     __shared__ int s_abort;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int lg = ilog2_small(a.pt_tile);
     const uint32_t q = a.q;
+    const int64_t npairs = (a.npts + 1) >> 1;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
@@ -435,7 +502,13 @@ pw_f16_kernel(PwArgs a)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&mbar)));
+        for (int s = 0; s < 2; s++) {
+            mbar_init(&full[s], F16_SPLIT_WARPS);
+            mbar_init(&empty[s], 1);
+            mbar_init(&tfull[s], 1);
+            mbar_init(&tempty[s], F16_EPI_WARPS);
+        }
+        mbar_init(&drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;");
         s_abort = 0;
     }
@@ -443,158 +516,195 @@ pw_f16_kernel(PwArgs a)
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = tmem_slot;
-    const uint32_t mbar_addr = (uint32_t)__cvta_generic_to_shared(&mbar);
+    volatile int *abort = &s_abort;
 
-    // digit split of one point into a stage (all threads); one warp writes one
-    // 8 x 8 core matrix (8 rows x 4 column pairs) per iteration: conflict-free.
-    // All 32 global loads of a lane are issued before any is used.
-    auto split = [&](int64_t pt, int stage) {
-        unsigned char *A01 = sm + stage * F16_STAGE;
-        unsigned char *A23 = A01 + F16_A_BYTES;
-        unsigned char *Bc = A23 + F16_A_BYTES;
+    if (warp >= F16_EPI_WARPS && warp < F16_MMA_WARP) {
+        // ---- loads and digit split: one warp writes one 8 x 8 core matrix per item
+        const int sw = warp - F16_EPI_WARPS;
         const int row_in = lane >> 2, kp = lane & 3;
-        constexpr int NIT = 64 / (F16_THREADS / 32);
-        uint32_t xa[NIT][2], yb[NIT][2];
+        const uint32_t biasA = 0x64806480u, biasB = 0x66006600u;   // 1152 and 1536 in both halves
+        int lc = 0;
+        for (int64_t gc = blockIdx.x; gc < npairs; gc += gridDim.x, lc++) {
+            const int64_t pt0 = 2 * gc;
+            const bool has1 = pt0 + 1 < a.npts;
+            uint2 va[8][2], vb[8][2];
 #pragma unroll
-        for (int itn = 0; itn < NIT; itn++) {
-            const int cmi = warp + itn * (F16_THREADS / 32);
-            const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
-            xa[itn][0] = (i < a.r && l < a.k) ? a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)] : 0u;
-            xa[itn][1] = (i < a.r && l + 1 < a.k) ? a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l + 1, lg, a.A.s_tile, a.s_e, a.s_p)] : 0u;
-            // B operand row n (output column), K index l (inner index)
-            const int n = i;
-            yb[itn][0] = (n < a.c && l < a.k) ? a.B.base[pw_off(pt, (int64_t)l * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)] : 0u;
-            yb[itn][1] = (n < a.c && l + 1 < a.k) ? a.B.base[pw_off(pt, (int64_t)(l + 1) * a.B.ld + n, lg, a.B.s_tile, a.s_e, a.s_p)] : 0u;
+            for (int itn = 0; itn < 8; itn++) {
+                const int cmi = sw + 8 * itn;
+                const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
+                const uint2 z = make_uint2(0u, 0u);
+                va[itn][0] = (i < a.r && l < a.k) ? f16_load_pair<TILE>(a.A, (int64_t)i * a.A.ld + l, pt0, has1, lg, a) : z;
+                va[itn][1] = (i < a.r && l + 1 < a.k) ? f16_load_pair<TILE>(a.A, (int64_t)i * a.A.ld + l + 1, pt0, has1, lg, a) : z;
+                vb[itn][0] = (i < a.c && l < a.k) ? f16_load_pair<TILE>(a.B, (int64_t)l * a.B.ld + i, pt0, has1, lg, a) : z;
+                vb[itn][1] = (i < a.c && l + 1 < a.k) ? f16_load_pair<TILE>(a.B, (int64_t)(l + 1) * a.B.ld + i, pt0, has1, lg, a) : z;
+            }
+#pragma unroll
+            for (int pp = 0; pp < 2; pp++) {
+                if (mbar_wait(&empty[pp], (uint32_t)((lc & 1) ^ 1), abort)) {
+                    unsigned char *A01 = sm + pp * F16_STAGE;
+                    unsigned char *Bc = A01 + 2 * F16_A_BYTES;
+#pragma unroll
+                    for (int itn = 0; itn < 8; itn++) {
+                        const int cmi = sw + 8 * itn;
+                        const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
+                        uint32_t h0[4], h1[4];
+                        digits4h(pp ? va[itn][0].y : va[itn][0].x, q, h0);
+                        digits4h(pp ? va[itn][1].y : va[itn][1].x, q, h1);
+#pragma unroll
+                        for (int d = 0; d < 4; d++)
+                            *reinterpret_cast<uint32_t *>(A01 + (d >> 1) * F16_A_BYTES + canon_off((d & 1) * 64 + i, l)) =
+                                unbias_pair(h0[d], h1[d], biasA);
+                        uint32_t g0[3], g1[3];
+                        digits3h(pp ? vb[itn][0].y : vb[itn][0].x, q, g0);
+                        digits3h(pp ? vb[itn][1].y : vb[itn][1].x, q, g1);
+                        const int rb = 96 * (i >> 5) + (i & 31);    // B row of output column i, digit 0
+#pragma unroll
+                        for (int j = 0; j < 3; j++)
+                            *reinterpret_cast<uint32_t *>(Bc + canon_off(rb + 32 * j, l)) = unbias_pair(g0[j], g1[j], biasB);
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[pp]);
+            }
         }
+    } else if (warp == F16_MMA_WARP) {
+        // ---- MMA issue (one thread)
+        if (lane == 0) {
+            const uint32_t idesc = (1u << 4) | ((uint32_t)(96 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+            uint32_t p = 0;
+            int lc = 0;
+            for (int64_t gc = blockIdx.x; gc < npairs; gc += gridDim.x, lc++) {
+                for (int pp = 0; pp < 2; pp++, p++) {
+                    bool ok = mbar_wait(&full[pp], (uint32_t)(lc & 1), abort);
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm + pp * F16_STAGE);
+                    for (int h = 0; h < 2; h++) {
+                        ok = ok && mbar_wait(&tempty[h], (p & 1) ^ 1, abort);
+                        if (!ok) break;
+                        asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-        for (int itn = 0; itn < NIT; itn++) {
-            const int cmi = warp + itn * (F16_THREADS / 32);
-            const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
-            int d0[4], d1[4];
-            digits4(xa[itn][0], q, d0);
-            digits4(xa[itn][1], q, d1);
-            const uint32_t o0 = canon_off(i, l), o1 = canon_off(64 + i, l);
-            *reinterpret_cast<uint32_t *>(A01 + o0) = pack_h2(d0[0], d1[0]);
-            *reinterpret_cast<uint32_t *>(A01 + o1) = pack_h2(d0[1], d1[1]);
-            *reinterpret_cast<uint32_t *>(A23 + o0) = pack_h2(d0[2], d1[2]);
-            *reinterpret_cast<uint32_t *>(A23 + o1) = pack_h2(d0[3], d1[3]);
-            int e0[3], e1[3];
-            digits3(yb[itn][0], q, e0);
-            digits3(yb[itn][1], q, e1);
+                        for (int s = 0; s < 2; s++)
 #pragma unroll
-            for (int j = 0; j < 3; j++)
-                *reinterpret_cast<uint32_t *>(Bc + canon_off(64 * j + i, l)) = pack_h2(e0[j], e1[j]);
+                            for (int ks = 0; ks < 4; ks++) {
+                                const uint64_t da = umma_desc(base + s * F16_A_BYTES + ks * 256);
+                                const uint64_t db = umma_desc(base + 2 * F16_A_BYTES + h * 12 * 1024 + ks * 256);
+                                asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                                             ::"r"(tmem + (uint32_t)(256 * h + 96 * s)), "l"(da), "l"(db), "r"(idesc),
+                                               "r"((uint32_t)(ks > 0)));
+                            }
+                        tc_commit(&tfull[h]);
+                    }
+                    if (ok) tc_commit(&empty[pp]);
+                }
+            }
+            // every MMA issued has completed before TMEM is released
+            tc_commit(&drain);
+            if (!mbar_wait(&drain, 0, nullptr)) *abort = 1;
         }
-    };
-
-    auto issue = [&](int stage) {
-        // one thread: the 2 x 4 MMAs of a point, then a commit to the mbarrier
-        const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm + stage * F16_STAGE);
-        const uint32_t idesc = (1u << 4) | ((uint32_t)(192 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+        __syncwarp();
+    } else {
+        // ---- epilogue: warp w reads TMEM lanes 32 (w & 3) + lane, columns half (w >> 2) of each region
+        const int sp = warp & 3, ch = warp >> 2, hi = sp >> 1;
+        const int i = (32 * sp + lane) & 63;
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * sp) << 16);
+        uint32_t w[2][3];
+        uint64_t koff = a.negoff;
 #pragma unroll
         for (int s = 0; s < 2; s++)
 #pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
-                const uint64_t da = umma_desc(base + s * F16_A_BYTES + ks * 256);
-                const uint64_t db = umma_desc(base + 2 * F16_A_BYTES + ks * 256);
-                const uint32_t acc = ks > 0;
-                asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
-                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
-                             ::"r"(tmem + (uint32_t)(s * 256)), "l"(da), "l"(db), "r"(idesc), "r"(acc));
+            for (int j = 0; j < 3; j++) {
+                w[s][j] = a.wd[2 * s + hi][j];
+                koff -= 0x4B400000ull * w[s][j];
             }
-        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar_addr)
-                     : "memory");
-    };
-
-    const int64_t stride = gridDim.x;
-    int64_t pt = blockIdx.x;
-    int it = 0;
-    if (pt < a.npts) {
-        split(pt, 0);
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (tid == 0) issue(0);
-    }
-    for (; pt < a.npts; pt += stride, it++) {
-        const int64_t nxt = pt + stride;
-        if (nxt < a.npts) {
-            split(nxt, (it + 1) & 1);
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        }
-        // wait for this point's MMAs (bounded)
-        {
-            uint32_t done = 0;
-            for (long long w = 0; w < F16_WAIT_LIMIT && !done; w++)
-                asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-                             : "=r"(done) : "r"(mbar_addr), "r"((uint32_t)(it & 1)) : "memory");
-            if (!done) s_abort = 1;
-        }
-        __syncthreads();
-        if (s_abort) {
-            if (tid == 0 && a.err) atomicExch(a.err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        // epilogue: warp w reads TMEM lanes 32 (w & 3) + lane, output columns [32 (w >> 2), +32)
-        {
-            const int L = 32 * (warp & 3) + lane;            // TMEM lane
-            const int i = L & 63, hi = L >> 6;                 // output row, digit parity
-            const int n0 = 32 * (warp >> 2);
-            const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+        uint32_t p = 0;
+        for (int64_t gc = blockIdx.x; gc < npairs; gc += gridDim.x) {
+            for (int pp = 0; pp < 2; pp++, p++) {
+                uint32_t *row = Cst + (pp * 2 + hi) * F16_CST_WORDS + i * F16_CST_LD;
+                for (int h = 0; h < 2; h++) {
+                    uint64_t acc[16];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int nb = n0 + 16 * h;
-                int64_t acc[16];
+                    for (int u = 0; u < 16; u++) acc[u] = 0;
+                    if (mbar_wait(&tfull[h], p & 1, abort)) {
+                        asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-                for (int u = 0; u < 16; u++) acc[u] = 0;
+                        for (int s = 0; s < 2; s++) {
+                            uint32_t v[3][16];
 #pragma unroll
-                for (int j = 0; j < 3; j++) {
-                    uint32_t v0[16], v1[16];
-                    TC_LD16(lane_base + (uint32_t)(64 * j + nb), v0);
-                    TC_LD16(lane_base + (uint32_t)(256 + 64 * j + nb), v1);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    const int64_t w0 = a.wd[hi][j], w1 = a.wd[2 + hi][j];
+                            for (int j = 0; j < 3; j++)
+                                TC_LD16(lane_base + (uint32_t)(256 * h + 96 * s + 32 * j + 16 * ch), v[j]);
+                            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int u = 0; u < 16; u++)
-                        acc[u] += (int64_t)__float2int_rn(__uint_as_float(v0[u])) * w0 +
-                                  (int64_t)__float2int_rn(__uint_as_float(v1[u])) * w1;
-                }
-                uint32_t r16[16];
+                            for (int j = 0; j < 3; j++)
 #pragma unroll
-                for (int u = 0; u < 16; u++)
-                    r16[u] = mod64_q((uint64_t)(acc[u] + (int64_t)a.negoff), q, a.r32, a.r32q, a.oneq);
-                // lanes 64..127 (odd digits) hand their partial sums to lanes 0..63
-                if (hi) {
-#pragma unroll
-                    for (int u = 0; u < 16; u++) P[i * 64 + nb + u] = r16[u];
-                }
-                __syncthreads();
-                if (!hi && i < a.r) {
-#pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        const int jcol = nb + u;
-                        if (jcol >= a.c) continue;
-                        uint32_t res = r16[u] + P[i * 64 + jcol];
-                        res = res >= q ? res - q : res;
-                        const int64_t off = pw_off(pt, (int64_t)i * a.ldc + jcol, lg, a.s_tile_c, a.s_e, a.s_p);
-                        if (a.accumulate) {
-                            res += a.C[off];
-                            res = res >= q ? res - q : res;
+                                for (int u = 0; u < 16; u++)
+                                    acc[u] += (uint64_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j][u]), 12582912.0f)) *
+                                              w[s][j];
                         }
-                        a.C[off] = res;
+                        asm volatile("tcgen05.fence::before_thread_sync;");
+                    }
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&tempty[h]);
+                    uint32_t r[16];
+#pragma unroll
+                    for (int u = 0; u < 16; u++) r[u] = mod64_q(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
+#pragma unroll
+                    for (int m = 0; m < 4; m++)
+                        *reinterpret_cast<uint4 *>(row + 32 * h + 16 * ch + 4 * m) =
+                            make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                }
+            }
+            asm volatile("bar.sync 1, %0;" ::"n"(F16_EPI_WARPS * 32) : "memory");
+            // write the pair: lanes along the entries of a row
+            const int64_t pt0 = 2 * gc;
+            const bool has1 = pt0 + 1 < a.npts;
+#pragma unroll 4
+            for (int m = 0; m < 16; m++) {
+                const int e = tid + F16_EPI_WARPS * 32 * m;
+                const int ii = e >> 6, n = e & 63;
+                if (ii >= a.r || n >= a.c) continue;
+                const int o = ii * F16_CST_LD + n;
+                uint32_t v0 = Cst[o] + Cst[F16_CST_WORDS + o];
+                uint32_t v1 = Cst[2 * F16_CST_WORDS + o] + Cst[3 * F16_CST_WORDS + o];
+                v0 = v0 >= q ? v0 - q : v0;
+                v1 = v1 >= q ? v1 - q : v1;
+                const int64_t ce = (int64_t)ii * a.ldc + n;
+                if (TILE) {
+                    uint2 *dst = reinterpret_cast<uint2 *>(a.C + ((pt0 >> 2) * a.s_tile_c + ce * 4 + (pt0 & 3)));
+                    if (a.accumulate) {
+                        const uint2 old = *dst;
+                        v0 += old.x;
+                        v1 += old.y;
+                        v0 = v0 >= q ? v0 - q : v0;
+                        v1 = v1 >= q ? v1 - q : v1;
+                    }
+                    *dst = make_uint2(v0, v1);
+                } else {
+                    uint32_t *d0 = a.C + pw_off(pt0, ce, lg, a.s_tile_c, a.s_e, a.s_p);
+                    if (a.accumulate) {
+                        v0 += *d0;
+                        v0 = v0 >= q ? v0 - q : v0;
+                    }
+                    *d0 = v0;
+                    if (has1) {
+                        uint32_t *d1 = a.C + pw_off(pt0 + 1, ce, lg, a.s_tile_c, a.s_e, a.s_p);
+                        if (a.accumulate) {
+                            v1 += *d1;
+                            v1 = v1 >= q ? v1 - q : v1;
+                        }
+                        *d1 = v1;
                     }
                 }
-                __syncthreads();
             }
+            asm volatile("bar.sync 2, %0;" ::"n"(F16_EPI_WARPS * 32) : "memory");
         }
-        asm volatile("tcgen05.fence::before_thread_sync;");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;");
-        if (nxt < a.npts && tid == 0) issue((it + 1) & 1);
     }
+
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (tid == 0 && s_abort && a.err) atomicExch(a.err, 1);
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(F16_TMEM_COLS));
 }
 
@@ -631,7 +741,8 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
     if (!attr_done) {
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_i8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i8));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc2));
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
         attr_done = true;
     }
     if (a.npts <= 0) return PMLG_OK;
@@ -644,9 +755,18 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
     } else if (f == PMLG_FORM_F16_TC) {
         PwArgs b = a;
         b.err = ctx->d_err;
-        const int64_t g3 = a.npts < ctx->sm_count ? a.npts : ctx->sm_count;
+        // point pairs share 8 aligned bytes in the point-tiled layout
+        const bool tile = a.pt_tile == 4 && a.s_e == 4 && a.s_p == 1 && (a.npts & 1) == 0 &&
+                          ((uintptr_t)a.A.base & 7) == 0 && ((uintptr_t)a.B.base & 7) == 0 &&
+                          ((uintptr_t)a.C & 7) == 0 && (a.A.s_tile & 1) == 0 && (a.B.s_tile & 1) == 0 &&
+                          (a.s_tile_c & 1) == 0;
+        const int64_t npairs = (a.npts + 1) / 2;
+        const int64_t g3 = npairs < ctx->sm_count ? npairs : ctx->sm_count;
         prof_begin(ctx, "pointwise_f16_tc", st);
-        pw_f16_kernel<<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        if (tile)
+            pw_f16_kernel<true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        else
+            pw_f16_kernel<false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
     } else {
         const int64_t items = (a.npts + 1) / 2;
         const int64_t g2 = items < ctx->sm_count ? items : ctx->sm_count;
