@@ -12,7 +12,8 @@
 // every 16 against bank conflicts).  Forward transforms are decimation in
 // frequency (natural order in, bit-reversed out), inverse ones decimation in
 // time (bit-reversed in, natural out): no reordering pass.  Values stay in
-// [0, 2q) between butterflies (q < 2^30, lazy reduction).
+// [0, 2q) between forward butterflies and in [0, 4q) between inverse ones
+// (q < 2^30, lazy reduction).
 #include "ntt.cuh"
 
 namespace pmlg {
@@ -24,30 +25,45 @@ __device__ __forceinline__ uint32_t csub(uint32_t x, uint32_t m) { return min(x,
 // Radix-2^G decimation-in-frequency butterflies on each of the 16 >> G
 // sub-transforms held by a thread, with the constant twiddles
 // w_{2^(G-l)}^(m mod half) = c16[(m mod half) * 16 / 2^(G-l)] of stage l.
-template <int G>
+//
+// ZH: the upper half of the input is zero (slot m + 8 of the first group), so
+// the first level is v[m + 8] = v[m] * w_16^m and v[m] is unchanged.
+// TW: every slot but 0 is multiplied by a group twiddle right after (a Shoup
+// product accepts any input below 2^32), so the last level leaves them in
+// [0, 4q) instead of reducing them to [0, 2q).
+template <int G, bool ZH = false, bool TW = false>
 __device__ __forceinline__ void dif_const(uint32_t (&v)[16], const NttDev &T)
 {
     constexpr int M = 1 << G, SUB = 16 >> G;
     const uint32_t q = T.q, q2 = 2 * q;
+    static_assert(!ZH || G == 4, "zero upper half only in a radix-16 group");
+    if constexpr (ZH) {
+        v[8] = v[0];
+#pragma unroll
+        for (int m = 1; m < 8; m++) v[m + 8] = shoup_mul(v[m], T.c16[m], T.c16q[m], q);
+    }
 #pragma unroll
     for (int u = 0; u < SUB; u++)
 #pragma unroll
-        for (int l = 0; l < G; l++) {
+        for (int l = ZH ? 1 : 0; l < G; l++) {
             const int half = M >> (l + 1);
+            const bool last = TW && l == G - 1;
 #pragma unroll
             for (int m = 0; m < M; m++) {
                 if (m & half) continue;
                 const int ti = (m % half) * (16 >> (G - l));
                 const uint32_t a = v[u * M + m], b = v[u * M + m + half];
-                v[u * M + m] = csub(a + b, q2);
+                v[u * M + m] = (last && m != 0) ? a + b : csub(a + b, q2);
                 const uint32_t d = a + q2 - b;
-                v[u * M + m + half] = ti ? shoup_mul(d, T.c16[ti], T.c16q[ti], q) : csub(d, q2);
+                v[u * M + m + half] = last ? d : ti ? shoup_mul(d, T.c16[ti], T.c16q[ti], q) : csub(d, q2);
             }
         }
 }
 
 // Radix-2^G decimation-in-time butterflies, constant twiddles
 // w_{2^(l+1)}^-(m mod 2^l) = c16[(m mod 2^l) * 16 / 2^(l+1)] (inverse table).
+// Lazy in the manner of Harvey: inputs and outputs lie in [0, 4q); only the
+// sum operand is brought to [0, 2q) before the butterfly.
 template <int G>
 __device__ __forceinline__ void dit_const(uint32_t (&v)[16], const NttDev &T)
 {
@@ -62,10 +78,10 @@ __device__ __forceinline__ void dit_const(uint32_t (&v)[16], const NttDev &T)
             for (int m = 0; m < M; m++) {
                 if (m & half) continue;
                 const int ti = (m % half) * (16 >> (l + 1));
-                const uint32_t a = v[u * M + m], b = v[u * M + m + half];
-                const uint32_t bw = ti ? shoup_mul(b, T.c16[ti], T.c16q[ti], q) : b;
-                v[u * M + m] = csub(a + bw, q2);
-                v[u * M + m + half] = csub(a + q2 - bw, q2);
+                const uint32_t a = csub(v[u * M + m], q2), b = v[u * M + m + half];
+                const uint32_t bw = ti ? shoup_mul(b, T.c16[ti], T.c16q[ti], q) : csub(b, q2);
+                v[u * M + m] = a + bw;
+                v[u * M + m + half] = a + q2 - bw;
             }
         }
 }
@@ -149,22 +165,23 @@ __device__ __forceinline__ void smem_to_regs_t(uint32_t (&v)[16], const uint32_t
     for (int s = 0; s < 16; s++) v[s] = p[grp_poff<G, LLS>(s)];
 }
 
-template <int LG, int GI>
+template <int LG, int GI, bool ZH>
 __device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
 {
     if constexpr (GI < FwdGeom<LG, 0>::NG) {
         using Gm = FwdGeom<LG, GI>;
+        constexpr bool TW = Gm::G == 4 && Gm::LLS > 0;
         if constexpr (GI > 0) {
             __syncthreads();
             smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
         }
-        dif_const<Gm::G>(v, T);
-        if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
+        dif_const<Gm::G, ZH && GI == 0, TW>(v, T);
+        if constexpr (TW) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
         if constexpr (GI < Gm::NG - 1) {
             __syncthreads();   // everyone done reading the previous layout
             regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
         }
-        fwd_groups<LG, GI + 1>(v, x, t, T);
+        fwd_groups<LG, GI + 1, ZH>(v, x, t, T);
     }
 }
 
@@ -187,8 +204,51 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
     }
 }
 
+// Registers per thread the kernels are compiled for (measured on GB300 at
+// N = 2^13: the forward transform is fastest at 32, the inverse at 40).
+#ifndef PMLG_NTT_FWD_REGS
+#define PMLG_NTT_FWD_REGS 32
+#endif
+#ifndef PMLG_NTT_INV_REGS
+#define PMLG_NTT_INV_REGS 40
+#endif
+
+// threads of a CTA: one transform of N/16 threads, at least 256
 template <int LG>
-__global__ void __launch_bounds__(1024)
+struct NttBlock
+{
+    static constexpr int TPT = 1 << (LG - 4);
+    static constexpr int THREADS = TPT >= 256 ? TPT : 256;
+    static constexpr int min_ctas(int regs) { return 65536 / (THREADS * regs) > 0 ? 65536 / (THREADS * regs) : 1; }
+    // resident CTAs the kernels ask registers for (per-thread register budgets above)
+    static constexpr int FWD_MIN = min_ctas(PMLG_NTT_FWD_REGS);
+    static constexpr int INV_MIN = min_ctas(PMLG_NTT_INV_REGS);
+};
+
+// Loads the first group (elements t + m N/16) and runs all groups; with ZH the
+// coefficients stop at N/2, so only slots 0..7 are read.
+template <int LG, bool ZH>
+__device__ __forceinline__ void fwd_transform(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T,
+                                              const NttFwdArgs &a, bool active, int64_t e)
+{
+    constexpr int TPT = 1 << (LG - 4);
+    const uint64_t *src = a.in + (active ? e : 0) * a.in_ld + a.in_off;
+    const int L = active ? (int)a.L : 0;
+#pragma unroll
+    for (int m = 0; m < (ZH ? 8 : 16); m++) {
+        const int d = t + m * TPT;
+        uint32_t val = 0;
+        if (d < L) {
+            const uint64_t s = src[d];
+            val = a.reduce ? mod64_q(s, T.q, T.r32, T.r32q, T.oneq) : (uint32_t)s;
+        }
+        v[m] = val;
+    }
+    fwd_groups<LG, 0, ZH>(v, x, t, T);
+}
+
+template <int LG>
+__global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::FWD_MIN)
 ntt_fwd_kernel(NttFwdArgs a)
 {
     extern __shared__ uint32_t smem[];
@@ -201,23 +261,11 @@ ntt_fwd_kernel(NttFwdArgs a)
     uint32_t *x = smem + sub * (N + (N >> 4));
     const bool active = e < a.nent;
 
-    // first group: elements t + m * N/16
     uint32_t v[16];
-    {
-        const uint64_t *src = a.in + (active ? e : 0) * a.in_ld + a.in_off;
-        const int L = active ? (int)a.L : 0;
-#pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int d = t + m * TPT;
-            uint32_t val = 0;
-            if (d < L) {
-                const uint64_t s = src[d];
-                val = a.reduce ? mod64_q(s, T.q, T.r32, T.r32q, T.oneq) : (uint32_t)s;
-            }
-            v[m] = val;
-        }
-    }
-    fwd_groups<LG, 0>(v, x, t, T);
+    if (2 * a.L <= N)
+        fwd_transform<LG, true>(v, x, t, T, a, active, e);
+    else
+        fwd_transform<LG, false>(v, x, t, T, a, active, e);
     // the last group leaves points 16t .. 16t+15 in v[0..15]
     if (active) {
         uint32_t *dst = a.out + j * a.prime_stride + e * kPtTile;
@@ -233,7 +281,7 @@ ntt_fwd_kernel(NttFwdArgs a)
 }
 
 template <int LG>
-__global__ void __launch_bounds__(1024)
+__global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INV_MIN)
 ntt_inv_kernel(NttInvArgs a)
 {
     extern __shared__ uint32_t smem[];
@@ -259,17 +307,33 @@ ntt_inv_kernel(NttInvArgs a)
         for (int m = 0; m < 16; m++) v[m] = 0;
     }
     inv_groups<LG, 0>(v, x, t, T);
-    // last group: element m of thread t is coefficient t + m * N/16
+    // last group: element m of thread t is coefficient t + m * N/16 (the factor
+    // 1/N was applied by the pointwise products)
     if (!active) return;
+    const uint32_t q = T.q;
+    const int64_t d0 = t - a.lo;
+    if (d0 >= 0 && d0 + 15 * TPT < a.cnt) {
+        // every slot of this thread is inside [lo, lo + cnt)
+        if (a.direct) {
+            uint64_t *o = a.out64 + e * a.out_ld + d0;
 #pragma unroll
-    for (int m = 0; m < 16; m++) {
-        const int64_t d = t + m * TPT - a.lo;
-        if (d < 0 || d >= a.cnt) continue;
-        const uint32_t val = csub(shoup_mul(v[m], T.ninv, T.ninvq, T.q), T.q);
-        if (a.direct)
-            a.out64[e * a.out_ld + d] = val;
-        else
-            a.res32[(j * a.nent + e) * a.cnt + d] = val;
+            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
+        } else {
+            uint32_t *o = a.res32 + (j * a.nent + e) * a.cnt + d0;
+#pragma unroll
+            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int64_t d = d0 + m * TPT;
+            if (d < 0 || d >= a.cnt) continue;
+            const uint32_t val = csub(csub(v[m], 2 * q), q);
+            if (a.direct)
+                a.out64[e * a.out_ld + d] = val;
+            else
+                a.res32[(j * a.nent + e) * a.cnt + d] = val;
+        }
     }
     if (a.direct)
         for (int64_t d = a.cnt + t; d < a.out_cap; d += TPT) a.out64[e * a.out_ld + d] = 0;

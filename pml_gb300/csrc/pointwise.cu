@@ -32,87 +32,6 @@ __device__ __forceinline__ int64_t pw_off(int64_t pt, int64_t e, int lg_tile, in
 __device__ __forceinline__ int ilog2_small(int x) { return 31 - __clz(x); }
 
 // ---------------------------------------------------------------------------
-// CUDA-core form
-// ---------------------------------------------------------------------------
-
-__global__ void __launch_bounds__(PW_THREADS)
-pw_cc_kernel(PwArgs a)
-{
-    extern __shared__ uint32_t sm[];
-    uint32_t *As = sm;                          // [PPC][64][CC_LD]  A[i][l]
-    uint32_t *Bs = sm + PW_PPC * 64 * CC_LD;    // [PPC][64][CC_LD]  B[l][j]
-    const int tid = threadIdx.x;
-    const int lg = ilog2_small(a.pt_tile);
-    const int64_t pt0 = (int64_t)blockIdx.x * PW_PPC;
-
-    for (int p = 0; p < PW_PPC; p++) {
-        const int64_t pt = pt0 + p;
-        const bool valid = pt < a.npts;
-        for (int idx = tid; idx < 64 * 64; idx += PW_THREADS) {
-            const int i = idx >> 6, l = idx & 63;
-            uint32_t va = 0, vb = 0;
-            if (valid && i < a.r && l < a.k)
-                va = a.A.base[pw_off(pt, (int64_t)i * a.A.ld + l, lg, a.A.s_tile, a.s_e, a.s_p)];
-            if (valid && i < a.k && l < a.c)
-                vb = a.B.base[pw_off(pt, (int64_t)i * a.B.ld + l, lg, a.B.s_tile, a.s_e, a.s_p)];
-            As[(p * 64 + i) * CC_LD + l] = va;
-            Bs[(p * 64 + i) * CC_LD + l] = vb;
-        }
-    }
-    __syncthreads();
-
-    const int ti = tid >> 4, tj = tid & 15;
-    const int kk = (a.k + 7) & ~7;
-    for (int p = 0; p < PW_PPC; p++) {
-        const int64_t pt = pt0 + p;
-        if (pt >= a.npts) break;
-        const uint32_t *Ap = As + p * 64 * CC_LD;
-        const uint32_t *Bp = Bs + p * 64 * CC_LD;
-        uint64_t acc[4][4];
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-#pragma unroll
-            for (int v = 0; v < 4; v++) acc[u][v] = 0;
-        for (int l0 = 0; l0 < kk; l0 += 8) {
-#pragma unroll
-            for (int l = l0; l < l0 + 8; l++) {
-                uint32_t av[4];
-#pragma unroll
-                for (int u = 0; u < 4; u++) av[u] = Ap[(4 * ti + u) * CC_LD + l];
-                const uint4 bv = *reinterpret_cast<const uint4 *>(&Bp[l * CC_LD + 4 * tj]);
-                const uint32_t b4[4] = {bv.x, bv.y, bv.z, bv.w};
-#pragma unroll
-                for (int u = 0; u < 4; u++)
-#pragma unroll
-                    for (int v = 0; v < 4; v++) acc[u][v] += (uint64_t)av[u] * b4[v];
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++)
-#pragma unroll
-                for (int v = 0; v < 4; v++)
-                    acc[u][v] = (acc[u][v] >> 32) * (uint64_t)a.r32 + (acc[u][v] & 0xffffffffull);
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++) {
-            const int i = 4 * ti + u;
-            if (i >= a.r) continue;
-#pragma unroll
-            for (int v = 0; v < 4; v++) {
-                const int j = 4 * tj + v;
-                if (j >= a.c) continue;
-                uint32_t res = mod64_q(acc[u][v], a.q, a.r32, a.r32q, a.oneq);
-                const int64_t off = pw_off(pt, (int64_t)i * a.ldc + j, lg, a.s_tile_c, a.s_e, a.s_p);
-                if (a.accumulate) {
-                    res += a.C[off];
-                    res = res >= a.q ? res - a.q : res;
-                }
-                a.C[off] = res;
-            }
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
 // INT8 tensor-core form
 // ---------------------------------------------------------------------------
 
@@ -213,7 +132,7 @@ pw_i8_kernel(PwArgs a)
                 uint64_t v = 0;
 #pragma unroll
                 for (int s = 0; s < 7; s++) v += (uint64_t)(uint32_t)acc[s][nt][r] * a.w8[s];
-                uint32_t res = mod64_q(v, a.q, a.r32, a.r32q, a.oneq);
+                uint32_t res = mod64_q(v, a.q, a.r32, a.r32q, a.oneq);   // w8 carries the output scale
                 const int64_t off = pw_off(pt, (int64_t)i * a.ldc + j, lg, a.s_tile_c, a.s_e, a.s_p);
                 if (a.accumulate) {
                     res += a.C[off];
@@ -321,6 +240,7 @@ pw_cc2_kernel(PwArgs a)
                     const int j = 4 * tj + v;
                     if (j >= a.c) continue;
                     uint32_t res = mod64_q(acc[u][v], a.q, a.r32, a.r32q, a.oneq);
+                    res = reduce_once(shoup_mul(res, a.scale, a.scaleq, a.q), a.q);
                     const int64_t off = pw_off(pt, (int64_t)i * a.ldc + j, lg, a.s_tile_c, a.s_e, a.s_p);
                     if (a.accumulate) {
                         res += a.C[off];
@@ -339,7 +259,7 @@ pw_cc2_kernel(PwArgs a)
 // FP16-digit tensor-core form (tcgen05.mma kind::f16, FP32 accumulators in TMEM)
 // ---------------------------------------------------------------------------
 //
-// Residues are centred (|x| < q/2 < 2^29) and written in balanced digits:
+// Residues are written in balanced digits (B entries centred first, |x| < q/2 < 2^29):
 //   A entries: 4 digits base 2^8,  |d_i| <= 128 ;  B entries: 3 digits base 2^10, |e_j| <= 512.
 // All digits are exact in FP16, every product d_i e_j is at most 2^16 in size,
 // and a sum over the 64 inner indices at most 2^22, so the FP32 accumulation
@@ -359,7 +279,8 @@ pw_cc2_kernel(PwArgs a)
 //                staging in shared memory, coalesced write of the pair;
 //   warps 8..15  loads of a point pair (the two points share 8 bytes in the
 //                point-tiled layout) and the digit split into two stages;
-//   warp 16      one thread issues the MMAs and commits to the mbarriers.
+//   warp 16      one thread issues the MMAs of a point into each region as
+//                soon as it is drained, and commits to the mbarriers.
 // Digits reach FP16 without conversion instructions: 0x6400 + u is the FP16
 // encoding of 1024 + u for 0 <= u <= 1024, and one packed subtraction removes
 // the bias.  The FP32 sums come back as integers the same way: for |S| <= 2^22
@@ -379,7 +300,11 @@ constexpr int F16_CST_LD = 68;                       // padded staging row (word
 constexpr int F16_CST_WORDS = 64 * F16_CST_LD;       // one (point, digit parity) plane
 constexpr int F16_SMEM = 2 * F16_STAGE + 4 * F16_CST_WORDS * 4 + 1024;   // + alignment slack
 constexpr uint32_t F16_TMEM_COLS = 512;
-constexpr long long F16_WAIT_LIMIT = 1ll << 20;      // try_wait polls; a legitimate wait lasts microseconds
+#ifndef PMLG_F16_SUSPEND_NS
+#define PMLG_F16_SUSPEND_NS 0
+#endif
+constexpr uint32_t F16_SUSPEND_NS = PMLG_F16_SUSPEND_NS;   // suspend-time hint per poll (0: none)
+constexpr uint64_t F16_WAIT_NS = 500000000ull;       // give up after 0.5 s; a legitimate wait lasts microseconds
 
 __device__ __forceinline__ uint32_t canon_off(int row, int k)
 {
@@ -405,17 +330,36 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *b)
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"((uint32_t)__cvta_generic_to_shared(b)) : "memory");
 }
 
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Bounded wait for the phase of the given parity; false when it gave up (or
-// another warp already did), in which case the abort flag is set.
+// another warp already did), in which case the abort flag is set.  With a
+// suspend-time hint the thread sleeps inside try_wait until the phase
+// completes or the hint expires.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort)
 {
     const uint32_t addr = (uint32_t)__cvta_generic_to_shared(b);
-    for (long long w = 0; w < F16_WAIT_LIMIT; w++) {
+    uint64_t t0 = 0;
+    for (int it = 0; it < (1 << 26); it++) {
         uint32_t done;
-        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
-                     : "=r"(done) : "r"(addr), "r"(parity) : "memory");
+        if (F16_SUSPEND_NS)
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done) : "r"(addr), "r"(parity), "r"(F16_SUSPEND_NS) : "memory");
+        else
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done) : "r"(addr), "r"(parity) : "memory");
         if (done) return true;
         if (abort && *abort) return false;
+        const uint64_t now = globaltimer_ns();
+        if (it == 0)
+            t0 = now;
+        else if (now - t0 > F16_WAIT_NS)
+            break;
     }
     if (abort) *abort = 1;
     return false;
@@ -427,39 +371,46 @@ __device__ __forceinline__ void tc_commit(uint64_t *b)
                  ::"r"((uint32_t)__cvta_generic_to_shared(b)) : "memory");
 }
 
-// FP16 encodings 0x6400 + (d + 128) of the balanced base-2^8 digits d of x (centred mod q)
-__device__ __forceinline__ void digits4h(uint32_t x, uint32_t q, uint32_t (&h)[4])
+// Digit planes of two A entries (same row, adjacent K) as half2 words, digit
+// i in word i.  With y = x + 0x80808080 (x < 2^30) the bytes b_i of y give
+// x = sum (b_i - 128) 256^i, |b_i - 128| <= 128; 0x6400 + b is the FP16
+// encoding of 1024 + b, and one packed subtraction of 1152 leaves b - 128.
+__device__ __forceinline__ void a_digit_pairs(uint32_t x0, uint32_t x1, uint32_t (&w)[4])
 {
-    int t = (int)(x > (q >> 1) ? x - q : x);
+    const uint32_t y0 = x0 + 0x80808080u, y1 = x1 + 0x80808080u;
 #pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const int tt = t + 128;
-        h[i] = (uint32_t)(tt & 255) + 0x6400u;
-        t = tt >> 8;
+    for (int i = 0; i < 4; i++) {
+        const uint32_t sel = (uint32_t)(i | (i << 4) | ((4 + i) << 8) | ((4 + i) << 12));
+        const uint32_t b = (__byte_perm(y0, y1, sel) & 0x00ff00ffu) | 0x64006400u;
+        asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(w[i]) : "r"(b), "r"(0x64806480u));
     }
-    h[3] = (uint32_t)(t + 128) + 0x6400u;
 }
 
-// FP16 encodings 0x6400 + (e + 512) of the balanced base-2^10 digits e of x (centred mod q);
-// the top digit lies in [-512, 512], so its encoding can reach 0x6800 (= 2048, still exact)
-__device__ __forceinline__ void digits3h(uint32_t x, uint32_t q, uint32_t (&h)[3])
+// Balanced base-2^10 digit planes of two B entries as half2 words.  The
+// centred residue t lies in (-2^29, 2^29), so y = t + 512 (1 + 2^10 + 2^20) has
+// two 10-bit fields f_0, f_1 and an 11-bit top field f_2 <= 1024 with
+// t = sum (f_j - 512) 2^(10 j); the encodings 0x6400 + f_j reach 0x6800 at
+// most (an addition, not an or, for the top field), minus 1536 gives f_j - 512.
+__device__ __forceinline__ void b_digit_pairs(uint32_t x0, uint32_t x1, uint32_t q, uint32_t (&w)[3])
 {
-    int t = (int)(x > (q >> 1) ? x - q : x);
+    const uint32_t h = q >> 1;
+    const uint32_t y0 = x0 + 0x20080200u - (x0 > h ? q : 0u);
+    const uint32_t y1 = x1 + 0x20080200u - (x1 > h ? q : 0u);
+    uint32_t b[3];
+    b[0] = (__byte_perm(y0, y1, 0x5410) & 0x03ff03ffu) | 0x64006400u;
+    b[1] = ((__byte_perm(y0, y1, 0x6521) >> 2) & 0x03ff03ffu) | 0x64006400u;
+    b[2] = ((__byte_perm(y0, y1, 0x7632) >> 4) & 0x07ff07ffu) + 0x64006400u;
 #pragma unroll
-    for (int j = 0; j < 2; j++) {
-        const int tt = t + 512;
-        h[j] = (uint32_t)(tt & 1023) + 0x6400u;
-        t = tt >> 10;
-    }
-    h[2] = (uint32_t)(t + 512) + 0x6400u;
+    for (int j = 0; j < 3; j++) asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(w[j]) : "r"(b[j]), "r"(0x66006600u));
 }
 
-// two biased FP16 encodings -> one half2 of the digit values
-__device__ __forceinline__ uint32_t unbias_pair(uint32_t h0, uint32_t h1, uint32_t bias2)
+// x mod q up to one multiple of q: x < 2^64, result in [0, 2q)
+__device__ __forceinline__ uint32_t mod64_q_2(uint64_t x, uint32_t q, uint32_t r32, uint32_t r32q, uint32_t oneq)
 {
-    uint32_t w = __byte_perm(h0, h1, 0x5410), r;
-    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(w), "r"(bias2));
-    return r;
+    const uint32_t t = shoup_mul((uint32_t)(x >> 32), r32, r32q, q);   // [0, 2q)
+    const uint32_t l = shoup_mul((uint32_t)x, 1u, oneq, q);             // [0, 2q)
+    const uint32_t s = t + l;                                           // < 4q < 2^32
+    return min(s, s - 2 * q);
 }
 
 #define TC_LD16(taddr, v)                                                                                       \
@@ -485,8 +436,10 @@ template <bool TILE>
 __global__ void __launch_bounds__(F16_THREADS, 1)
 pw_f16_kernel(PwArgs a)
 {
-    extern __shared__ unsigned char f16_raw[];
-    unsigned char *sm = (unsigned char *)(((uintptr_t)f16_raw + 1023) & ~(uintptr_t)1023);
+    extern __shared__ __align__(16) unsigned char f16_raw[];
+    // 1024-byte aligned start, by pointer arithmetic on the shared array (the
+    // accesses stay shared-memory instructions)
+    unsigned char *sm = f16_raw + ((1024u - ((uint32_t)__cvta_generic_to_shared(f16_raw) & 1023u)) & 1023u);
     uint32_t *Cst = (uint32_t *)(sm + 2 * F16_STAGE);
     __shared__ __align__(8) uint64_t full[2], empty[2], tfull[2], tempty[2], drain;
     __shared__ uint32_t tmem_slot;
@@ -522,7 +475,6 @@ pw_f16_kernel(PwArgs a)
         // ---- loads and digit split: one warp writes one 8 x 8 core matrix per item
         const int sw = warp - F16_EPI_WARPS;
         const int row_in = lane >> 2, kp = lane & 3;
-        const uint32_t biasA = 0x64806480u, biasB = 0x66006600u;   // 1152 and 1536 in both halves
         int lc = 0;
         for (int64_t gc = blockIdx.x; gc < npairs; gc += gridDim.x, lc++) {
             const int64_t pt0 = 2 * gc;
@@ -547,20 +499,16 @@ pw_f16_kernel(PwArgs a)
                     for (int itn = 0; itn < 8; itn++) {
                         const int cmi = sw + 8 * itn;
                         const int i = (cmi >> 3) * 8 + row_in, l = (cmi & 7) * 8 + 2 * kp;
-                        uint32_t h0[4], h1[4];
-                        digits4h(pp ? va[itn][0].y : va[itn][0].x, q, h0);
-                        digits4h(pp ? va[itn][1].y : va[itn][1].x, q, h1);
+                        uint32_t wa[4], wb[3];
+                        a_digit_pairs(pp ? va[itn][0].y : va[itn][0].x, pp ? va[itn][1].y : va[itn][1].x, wa);
 #pragma unroll
                         for (int d = 0; d < 4; d++)
-                            *reinterpret_cast<uint32_t *>(A01 + (d >> 1) * F16_A_BYTES + canon_off((d & 1) * 64 + i, l)) =
-                                unbias_pair(h0[d], h1[d], biasA);
-                        uint32_t g0[3], g1[3];
-                        digits3h(pp ? vb[itn][0].y : vb[itn][0].x, q, g0);
-                        digits3h(pp ? vb[itn][1].y : vb[itn][1].x, q, g1);
+                            *reinterpret_cast<uint32_t *>(A01 + (d >> 1) * F16_A_BYTES + canon_off((d & 1) * 64 + i, l)) = wa[d];
+                        b_digit_pairs(pp ? vb[itn][0].y : vb[itn][0].x, pp ? vb[itn][1].y : vb[itn][1].x, q, wb);
                         const int rb = 96 * (i >> 5) + (i & 31);    // B row of output column i, digit 0
 #pragma unroll
                         for (int j = 0; j < 3; j++)
-                            *reinterpret_cast<uint32_t *>(Bc + canon_off(rb + 32 * j, l)) = unbias_pair(g0[j], g1[j], biasB);
+                            *reinterpret_cast<uint32_t *>(Bc + canon_off(rb + 32 * j, l)) = wb[j];
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 }
@@ -577,10 +525,9 @@ pw_f16_kernel(PwArgs a)
             for (int64_t gc = blockIdx.x; gc < npairs; gc += gridDim.x, lc++) {
                 for (int pp = 0; pp < 2; pp++, p++) {
                     bool ok = mbar_wait(&full[pp], (uint32_t)(lc & 1), abort);
-                    asm volatile("tcgen05.fence::after_thread_sync;");
                     const uint32_t base = (uint32_t)__cvta_generic_to_shared(sm + pp * F16_STAGE);
                     for (int h = 0; h < 2; h++) {
-                        ok = ok && mbar_wait(&tempty[h], (p & 1) ^ 1, abort);
+                        ok = ok && mbar_wait(&tempty[h], (p & 1) ^ 1, abort);   // region h of point p - 1 drained
                         if (!ok) break;
                         asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
@@ -648,7 +595,7 @@ pw_f16_kernel(PwArgs a)
                     if (lane == 0) mbar_arrive(&tempty[h]);
                     uint32_t r[16];
 #pragma unroll
-                    for (int u = 0; u < 16; u++) r[u] = mod64_q(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
+                    for (int u = 0; u < 16; u++) r[u] = mod64_q_2(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
 #pragma unroll
                     for (int m = 0; m < 4; m++)
                         *reinterpret_cast<uint4 *>(row + 32 * h + 16 * ch + 4 * m) =
@@ -665,8 +612,11 @@ pw_f16_kernel(PwArgs a)
                 const int ii = e >> 6, n = e & 63;
                 if (ii >= a.r || n >= a.c) continue;
                 const int o = ii * F16_CST_LD + n;
+                // the two digit-parity halves, each in [0, 2q)
                 uint32_t v0 = Cst[o] + Cst[F16_CST_WORDS + o];
                 uint32_t v1 = Cst[2 * F16_CST_WORDS + o] + Cst[3 * F16_CST_WORDS + o];
+                v0 = min(v0, v0 - 2 * q);
+                v1 = min(v1, v1 - 2 * q);
                 v0 = v0 >= q ? v0 - q : v0;
                 v1 = v1 >= q ? v1 - q : v1;
                 const int64_t ce = (int64_t)ii * a.ldc + n;
@@ -712,19 +662,23 @@ pw_f16_kernel(PwArgs a)
 // host side
 // ---------------------------------------------------------------------------
 
-void pointwise_set_modulus(PwArgs &a, uint32_t q)
+void pointwise_set_modulus(PwArgs &a, uint32_t q, uint32_t scale)
 {
     a.q = q;
     a.r32 = (uint32_t)((1ull << 32) % q);
     a.r32q = h_shoup_q(a.r32, q);
     a.oneq = (uint32_t)((1ull << 32) / q);
-    uint64_t w = 1;
+    a.scale = scale % q;
+    a.scaleq = h_shoup_q(a.scale, q);
+    // the recombination weights of the tensor-core forms carry the scale for free
+    uint64_t w = a.scale;
     for (int s = 0; s < 7; s++) {
-        a.w8[s] = (uint32_t)(w % q);
+        a.w8[s] = (uint32_t)w;
         w = (w << 8) % q;
     }
     for (int i = 0; i < 4; i++)
-        for (int j = 0; j < 3; j++) a.wd[i][j] = (uint32_t)h_powmod(2, (uint64_t)(8 * i + 10 * j), q);
+        for (int j = 0; j < 3; j++)
+            a.wd[i][j] = (uint32_t)((unsigned __int128)h_powmod(2, (uint64_t)(8 * i + 10 * j), q) * a.scale % q);
     a.negoff = ((1ull << 56) / q + 1) * q;
 }
 

@@ -26,8 +26,9 @@ struct PwArgs
     int64_t npts;
     int r, k, c;        // block shape, each <= 64
     uint32_t q, r32, r32q, oneq;
-    uint32_t w8[7];     // 2^(8s) mod q for the limb recombination
-    uint32_t wd[4][3];  // 2^(8i + 10j) mod q for the FP16-digit recombination
+    uint32_t scale, scaleq;   // every product is multiplied by scale (N^-1 ahead of an inverse NTT)
+    uint32_t w8[7];     // scale * 2^(8s) mod q for the limb recombination
+    uint32_t wd[4][3];  // scale * 2^(8i + 10j) mod q for the FP16-digit recombination
     uint64_t negoff;    // multiple of q >= 2^56, makes signed digit sums non-negative
     int accumulate;     // C += A*B instead of C = A*B
     int *err;           // device error word (bounded waits that gave up), may be null
@@ -37,8 +38,9 @@ struct PwArgs
 // by the caller.
 int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st);
 
-// Fills the modulus-dependent fields of PwArgs.
-void pointwise_set_modulus(PwArgs &a, uint32_t q);
+// Fills the modulus-dependent fields of PwArgs; the products come out
+// multiplied by `scale` (1 for plain matrix products).
+void pointwise_set_modulus(PwArgs &a, uint32_t q, uint32_t scale = 1);
 
 // Products with r, k, c of any size: splits into 64 x 64 blocks and
 // accumulates over the inner blocks.

@@ -79,7 +79,7 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
         pa.s_p = 1;
         pa.npts = N;
         pa.accumulate = 0;
-        pointwise_set_modulus(pa, plan.q[i]);
+        pointwise_set_modulus(pa, plan.q[i], tabs[i]->ninv);   // the 1/N of the inverse transform
         PMLG_TRY(pointwise_blocked(ctx, pa, j.r, j.k, j.c, form, st));
     }
 
