@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--impl", choices=["pml", "reference"], default="pml")
     ap.add_argument("--no-pmbasis", action="store_true", help="skip the pmbasis measurement")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the pointwise-batch and batched-uneven measurements")
     ap.add_argument("--profile-case", choices=["product", "pmbasis"], default=None,
                     help="run one product per form (or one pmbasis at order 1024) and exit: "
                          "the small case for kernel captures")
@@ -238,6 +240,102 @@ def algorithmic_bytes(kernel: str):
     return ("hbm", None)
 
 
+def is_prime64(n: int) -> bool:
+    """Deterministic Miller-Rabin for n < 2^64 (bases: the first 12 primes)."""
+    if n < 2:
+        return False
+    small = (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37)
+    for q in small:
+        if n % q == 0:
+            return n == q
+    d, s = n - 1, 0
+    while d % 2 == 0:
+        d //= 2
+        s += 1
+    for a in small:
+        x = pow(a, d, n)
+        if x in (1, n - 1):
+            continue
+        for _ in range(s - 1):
+            x = x * x % n
+            if x == n - 1:
+                break
+        else:
+            return False
+    return True
+
+
+def random_prime(bits: int, rng) -> int:
+    while True:
+        n = int(rng.integers(1 << (bits - 1), 1 << bits, dtype=np.uint64)) | 1
+        if is_prime64(n):
+            return n
+
+
+def _time_calls(fn, st, reps: int, warm: int):
+    import torch
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        out = fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def measure_pointwise_batch(ctx, dev, st, forms, rank):
+    """4096 independent products 64x64 . 64x64 mod p = 998244353, uint32 storage, one
+    pmlg_nmod_mat_mul_batch_u32 call per form (the pointwise contraction alone)."""
+    import torch
+    import pml_gb300
+    nb = 4096
+    rng = np.random.default_rng(11 + rank)
+    A = torch.from_numpy(rng.integers(0, P, size=(nb, 64, 64), dtype=np.uint32).view(np.int32)).to(dev)
+    B = torch.from_numpy(rng.integers(0, P, size=(nb, 64, 64), dtype=np.uint32).view(np.int32)).to(dev)
+    res, outs = {}, {}
+    for name, form in forms:
+        ctx.set_form(form)
+        ms, out = _time_calls(lambda: pml_gb300.nmod_mat_mul_batch(A, B, P, ctx=ctx), st, 5, 2)
+        res[name + "_ms"] = ms
+        res[name + "_gmac_per_s"] = nb * 64 ** 3 / ms / 1e6
+        outs[name] = out
+    res["forms_agree"] = all(bool(torch.equal(outs["cuda_core"], o)) for o in outs.values())
+    res["config"] = "4096 products 64x64 . 64x64 mod 998244353, uint32 entries uniform in [0, p), batch-major"
+    return res
+
+
+def measure_batched_uneven(ctx, dev, st, forms, rank):
+    """256 independent nmod_poly_mat_mul instances in one pmlg_poly_mat_mul_batch call: square
+    sizes m uniform in {4..48}, lengths 2^U(6,12), half p = 998244353, half seeded 59-bit primes."""
+    import torch
+    import pml_gb300
+    rng = np.random.default_rng(5 + rank)
+    jobs, macs = [], 0
+    for i in range(256):
+        m = int(rng.integers(4, 49))
+        ln = int(2 ** rng.uniform(6, 12))
+        p = P if i % 2 == 0 else random_prime(59, rng)
+        A = torch.from_numpy(rng.integers(0, p, size=(m, m, ln), dtype=np.uint64).view(np.int64)).to(dev)
+        B = torch.from_numpy(rng.integers(0, p, size=(m, m, ln), dtype=np.uint64).view(np.int64)).to(dev)
+        jobs.append((A, B, p))
+        macs += m ** 3 * ln
+    res, outs = {}, {}
+    for name, form in forms:
+        ctx.set_form(form)
+        ms, out = _time_calls(lambda: pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx), st, 3, 1)
+        res[name + "_ms"] = ms
+        outs[name] = out
+    res["forms_agree"] = all(all(bool(torch.equal(a, b)) for a, b in zip(outs["cuda_core"], o))
+                             for o in outs.values())
+    res["config"] = ("256 instances, m uniform in {4..48}, length 2^U(6,12), half p = 998244353, "
+                     "half seeded 59-bit primes (CRT over NTT primes), uniform coefficients")
+    res["coefficient_macs"] = macs
+    return res
+
+
 def run_pml(args):
     import torch
     rank, world, local = dist_env()
@@ -409,6 +507,13 @@ def run_pml(args):
         pm["config"] = "pmbasis 64x32, order 8192, zero shift, p = 998244353, uniform coefficients"
         pm["timing"] = "wall clock around one call (it synchronises internally), after one warm-up call"
 
+    # the two other GPU workloads of the benchmark set: the pointwise contraction alone and the
+    # batched uneven products (every form, CUDA events around each call)
+    extra = {} if args.no_extra else {
+        "pointwise_batch": measure_pointwise_batch(ctx, dev, st, FORMS, rank),
+        "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
+    }
+
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -436,6 +541,7 @@ def run_pml(args):
             "kernels": {name: summarize(pr) for name, pr in profs.items()},
             "clocks": clocks,
             "pmbasis": pm,
+            **extra,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

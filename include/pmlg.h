@@ -72,6 +72,19 @@ PMLG_API int pmlg_ctx_set_leaf_order(pmlg_ctx *ctx, int64_t order);
 /* number of kernels this context has launched so far */
 PMLG_API unsigned long long pmlg_ctx_launch_count(const pmlg_ctx *ctx);
 PMLG_API const char *pmlg_ctx_last_error(const pmlg_ctx *ctx);
+/* Failure detection: every device-side wait of the kernels (mbarrier phases,
+ * published eliminations) is bounded; a wait that gives up sets the context's
+ * device error word and the kernel returns.  device_status synchronises
+ * `stream`, reads and clears the word, and returns PMLG_ETIMEOUT if it was set
+ * (the results since the previous check are then invalid).  The host-buffer
+ * entry points and pmbasis/mbasis check it before they return; callers of the
+ * stream-ordered device entry points call it when they synchronise.  No
+ * reference counterpart: the reference has no device and aborts on errors. */
+PMLG_API int pmlg_ctx_device_status(pmlg_ctx *ctx, void *stream);
+/* Diagnostic: a kernel waits (at most wait_ns, <= 1 s) on an mbarrier phase
+ * that nothing completes and reports through the error word; returns
+ * PMLG_ETIMEOUT from device_status, with the context still usable. */
+PMLG_API int pmlg_ctx_selftest_timeout(pmlg_ctx *ctx, unsigned long long wait_ns, void *stream);
 /* Kernel timing (tracing): when on, every kernel launched through the context
  * is bracketed by CUDA events recorded on its own stream.  set_profiling also
  * clears the records.  profile_read synchronises on the recorded events and

@@ -29,6 +29,8 @@ SIGNATURES = {
     "pmlg_ctx_set_leaf_order": (C.c_int, [_vp, _i64]),
     "pmlg_ctx_launch_count": (C.c_ulonglong, [_vp]),
     "pmlg_ctx_last_error": (C.c_char_p, [_vp]),
+    "pmlg_ctx_device_status": (C.c_int, [_vp, _vp]),
+    "pmlg_ctx_selftest_timeout": (C.c_int, [_vp, C.c_ulonglong, _vp]),
     "pmlg_ctx_set_profiling": (C.c_int, [_vp, C.c_int]),
     "pmlg_ctx_profile_read": (C.c_int, [_vp, C.c_char_p, C.c_size_t, C.POINTER(C.c_double),
                                         C.POINTER(C.c_ulonglong), C.c_int, C.POINTER(C.c_int)]),

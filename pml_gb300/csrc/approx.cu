@@ -41,6 +41,7 @@ struct LeafArgs
     uint32_t p, r32, r32q, oneq;
     uint32_t pneg;    // -p^{-1} mod 2^32 (Montgomery reduction)
     uint32_t r2;      // 2^64 mod p (Montgomery conversion)
+    int *err;         // device error word: a bounded wait gave up
 };
 
 __device__ __forceinline__ uint32_t mulmod32(uint32_t a, uint32_t b, const LeafArgs &A)
@@ -277,10 +278,11 @@ mbasis_leaf_kernel(LeafArgs a)
 //      CTA 0's shared memory (distributed shared memory stores); cluster barrier;
 //   3. CTA 0 runs the elimination with its 16 warps: lane j holds row j of
 //      E = R[ord]^T (j < n <= 32), warp w holds columns [4w, 4w+4) in
-//      registers; column c's owner warp finds the pivot with a ballot and
-//      publishes it through shared memory (double-buffered, one barrier per
-//      column); every warp updates its columns with pivot row values taken by
-//      warp shuffles.  Updates are division-free,
+//      registers (LC_EW = 16 warps of 4 columns by default); column c's owner
+//      warp finds the pivot with a ballot and publishes it through shared
+//      memory (double-buffered, one barrier per column); every warp updates
+//      its columns with pivot row values taken by warp shuffles.  Updates are
+//      division-free,
 //      row_j <- (pv * row_j - f_j * row_pl) * 2^-32 mod p (Montgomery
 //      reduction): every row operation only scales rows, so the ratios
 //      E[pl_b][np_a] / E[pl_b][pc_b] at the end are the RREF entries.  Once
@@ -296,6 +298,12 @@ mbasis_leaf_kernel(LeafArgs a)
 constexpr int LC_CL = 8;
 constexpr int LC_THREADS = 512;
 constexpr int LC_MAXM = 64, LC_MAXN = 32, LC_MAXORD = 32;
+#ifndef PMLG_LC_ELIM_WARPS
+#define PMLG_LC_ELIM_WARPS 16
+#endif
+// warps of CTA 0 that run the elimination (each holds 64 / LC_EW columns of E)
+constexpr int LC_EW = PMLG_LC_ELIM_WARPS, LC_CPW = LC_MAXM / LC_EW;
+static_assert(LC_EW == 4 || LC_EW == 8 || LC_EW == 16, "elimination warps");
 
 __device__ __forceinline__ uint32_t redc(uint64_t t, uint32_t p, uint32_t pneg)
 {
@@ -328,8 +336,8 @@ struct LcShared
     int growf[LC_CL];                   // CTA 0: per-CTA "pivot row at the top coefficient" flags
     long long sh[LC_MAXM];
     int perm[LC_MAXM];
-    uint32_t fbuf[2][32];
-    uint32_t pvbuf[2];
+    uint32_t fbuf[2][32];               // the current column's values, pivot value and
+    uint32_t pvbuf[2];                  // pivot lane (double-buffered by column)
     int plbuf[2];
     int pivlane[LC_MAXM], pivcol[LC_MAXM], nonpiv[LC_MAXM];
     uint32_t inv[LC_MAXM];
@@ -341,7 +349,7 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     __shared__ LcShared S;
-    extern __shared__ uint32_t dyn[];
+    extern __shared__ __align__(16) uint32_t dyn[];
     const int c = (int)cluster.block_rank();
     const int tid = threadIdx.x, nth = blockDim.x;
     const int m = a.m, n = a.n, order = a.order;
@@ -350,10 +358,12 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     const int m0 = c * ncm, n0 = c * ncn;
     const int cm = m0 < m ? (m - m0 < ncm ? m - m0 : ncm) : 0;
     const int cn = n0 < n ? (n - n0 < ncn ? n - n0 : ncn) : 0;
-    // coefficient d of the slices starts at d * sab (appbas) and d * sr (R): the
-    // strides are odd, so threads working on consecutive coefficients of the
-    // same row hit distinct banks
-    const int sab = m * ncm + 1, sr = m * ncn + 1;
+    // coefficient d of the slices starts at d * sab (appbas) and d * sr (R).  The
+    // padding makes threads working on consecutive coefficients of the same row
+    // hit distinct banks: 4 words when the slice rows are whole 16-byte vectors
+    // (the update then moves rows with 128-bit accesses), 1 word otherwise
+    const bool vec = (ncm & 3) == 0 && (ncn & 3) == 0;
+    const int sab = m * ncm + (vec ? 4 : 1), sr = m * ncn + (vec ? 4 : 1);
     uint32_t *AB = dyn;                                      // [order+1][m][ncm], padded
     uint32_t *R = dyn + (size_t)(order + 1) * sab;           // [order][m][ncn], padded
     const int64_t fl = a.flen < order ? a.flen : order;
@@ -398,56 +408,64 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         }
         cluster.sync();
 
-        // 3. elimination in CTA 0 (all 16 warps)
+        // 3. elimination in CTA 0 (its first LC_EW warps)
         if (c == 0) {
             const int w = tid >> 5, lane = tid & 31;
-            uint32_t x[4];
-#pragma unroll
-            for (int k = 0; k < 4; k++) x[k] = (lane < n && 4 * w + k < m) ? S.E[lane][4 * w + k] : 0u;
-            unsigned used = 0;
             int rank = 0, nn = 0;
-            for (int col = 0; col < m; col++) {
-                if (rank == n) {
-                    // every row holds a pivot: the remaining columns are non-pivots
-                    if (tid == 0) S.nonpiv[nn] = col;
-                    nn++;
-                    continue;
-                }
-                const int buf = col & 1, cw = col >> 2, cl = col & 3;
-                if (w == cw) {
-                    uint32_t v = x[0];
-                    if (cl == 1) v = x[1];
-                    if (cl == 2) v = x[2];
-                    if (cl == 3) v = x[3];
-                    const unsigned cand = __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
-                    const int pl = cand ? __ffs(cand) - 1 : -1;
-                    S.fbuf[buf][lane] = v;
-                    if (lane == 0) S.plbuf[buf] = pl;
-                    if (lane == pl) S.pvbuf[buf] = v;
-                }
-                __syncthreads();
-                const int pl = S.plbuf[buf];
-                if (pl < 0) {
-                    if (tid == 0) S.nonpiv[nn] = col;
-                    nn++;
-                    continue;
-                }
-                const uint32_t pv = S.pvbuf[buf];
-                const uint32_t f = S.fbuf[buf][lane];
-                const uint32_t nf = f ? p - f : 0u;
+            if (w < LC_EW) {
+                uint32_t x[LC_CPW];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
-                    if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
+                for (int k = 0; k < LC_CPW; k++)
+                    x[k] = (lane < n && LC_CPW * w + k < m) ? S.E[lane][LC_CPW * w + k] : 0u;
+                unsigned used = 0;
+                for (int col = 0; col < m; col++) {
+                    if (rank == n) {
+                        // every row holds a pivot: the remaining columns are non-pivots
+                        if (tid == 0) S.nonpiv[nn] = col;
+                        nn++;
+                        continue;
+                    }
+                    const int buf = col & 1, cw = col / LC_CPW, cl = col % LC_CPW;
+                    if (w == cw) {
+                        uint32_t v = x[0];
+#pragma unroll
+                        for (int k = 1; k < LC_CPW; k++)
+                            if (cl == k) v = x[k];
+                        const unsigned cand = __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
+                        const int pl = cand ? __ffs(cand) - 1 : -1;
+                        S.fbuf[buf][lane] = v;
+                        if (lane == 0) S.plbuf[buf] = pl;
+                        if (lane == pl) S.pvbuf[buf] = v;
+                    }
+                    if (LC_EW == 16)
+                        __syncthreads();
+                    else
+                        asm volatile("bar.sync 1, %0;" ::"n"(LC_EW * 32) : "memory");
+                    const int pl = S.plbuf[buf];
+                    if (pl < 0) {
+                        if (tid == 0) S.nonpiv[nn] = col;
+                        nn++;
+                        continue;
+                    }
+                    const uint32_t pv = S.pvbuf[buf];
+                    const uint32_t f = S.fbuf[buf][lane];
+                    const uint32_t nf = f ? p - f : 0u;
+#pragma unroll
+                    for (int k = 0; k < LC_CPW; k++) {
+                        const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
+                        if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
+                    }
+                    used |= 1u << pl;
+                    if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
+                    rank++;
                 }
-                used |= 1u << pl;
-                if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
-                rank++;
+#pragma unroll
+                for (int k = 0; k < LC_CPW; k++)
+                    if (lane < n && LC_CPW * w + k < m) S.E[lane][LC_CPW * w + k] = x[k];
             }
-#pragma unroll
-            for (int k = 0; k < 4; k++)
-                if (lane < n && 4 * w + k < m) S.E[lane][4 * w + k] = x[k];
+            if (tid == 0) S.info[0] = rank;
             __syncthreads();
+            rank = S.info[0];
             const int nullity = m - rank;
             if (rank > 0 && nullity > 0) {
                 if (tid < rank) {
@@ -527,6 +545,45 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
             uint32_t *base = isab ? AB + (size_t)d * sab : R + (size_t)d * sr;
             uint32_t *dst = base + S.nprow[ia] * width;
             uint64_t acc[8];
+            if (vec) {
+                // whole rows of 4 or 8 words (columns past `cols` are zero padding)
+                const int nq = width >> 2;
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    if (h < nq) {
+                        const uint4 v = *reinterpret_cast<const uint4 *>(dst + 4 * h);
+                        acc[4 * h] = v.x; acc[4 * h + 1] = v.y; acc[4 * h + 2] = v.z; acc[4 * h + 3] = v.w;
+                    } else {
+                        acc[4 * h] = acc[4 * h + 1] = acc[4 * h + 2] = acc[4 * h + 3] = 0;
+                    }
+                for (int b0 = 0; b0 < rank; b0 += 8) {
+                    const int bend = b0 + 8 < rank ? b0 + 8 : rank;
+                    for (int b = b0; b < bend; b++) {
+                        const uint64_t xv = S.X[ia][b];
+                        const uint32_t *src = base + S.pivrow[b] * width;
+#pragma unroll
+                        for (int h = 0; h < 2; h++)
+                            if (h < nq) {
+                                const uint4 v = *reinterpret_cast<const uint4 *>(src + 4 * h);
+                                acc[4 * h] += xv * v.x; acc[4 * h + 1] += xv * v.y;
+                                acc[4 * h + 2] += xv * v.z; acc[4 * h + 3] += xv * v.w;
+                            }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
+                }
+#pragma unroll
+                for (int h = 0; h < 2; h++)
+                    if (h < nq) {
+                        uint4 v;
+                        v.x = mod64_q(acc[4 * h], p, a.r32, a.r32q, a.oneq);
+                        v.y = mod64_q(acc[4 * h + 1], p, a.r32, a.r32q, a.oneq);
+                        v.z = mod64_q(acc[4 * h + 2], p, a.r32, a.r32q, a.oneq);
+                        v.w = mod64_q(acc[4 * h + 3], p, a.r32, a.r32q, a.oneq);
+                        *reinterpret_cast<uint4 *>(dst + 4 * h) = v;
+                    }
+                continue;
+            }
 #pragma unroll
             for (int u = 0; u < 8; u++) acc[u] = (u < cols) ? dst[u] : 0ull;
             for (int b0 = 0; b0 < rank; b0 += 8) {
@@ -585,7 +642,8 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
 static size_t leaf_cluster_smem(int m, int n, int order)
 {
     const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
-    return ((size_t)(order + 1) * (m * ncm + 1) + (size_t)order * (m * ncn + 1)) * sizeof(uint32_t);
+    const int pad = ((ncm & 3) == 0 && (ncn & 3) == 0) ? 4 : 1;   // as in the kernel
+    return ((size_t)(order + 1) * (m * ncm + pad) + (size_t)order * (m * ncn + pad)) * sizeof(uint32_t);
 }
 
 // ---------------------------------------------------------------------------
@@ -639,6 +697,7 @@ static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, i
     a.out = out; a.ldo = ldo;
     a.R = R; a.AB = AB;
     a.shift = S.d_shift;
+    a.err = S.ctx->d_err;
     a.m = (int)S.m; a.n = (int)S.n; a.order = (int)order;
     a.p = (uint32_t)S.p;
     a.r32 = (uint32_t)((1ull << 32) % S.p);
@@ -784,7 +843,7 @@ static int approx_entry(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *s
         PMLG_TRY(pmbasis_rec(S, appbas, cap, F, flen, flen, order, &len));
     }
     PMLG_CUDA_TRY(cudaMemcpyAsync(shift, S.d_shift, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
-    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    PMLG_TRY(device_status(ctx, st));
     if (out_len) *out_len = len;
     return PMLG_OK;
 }

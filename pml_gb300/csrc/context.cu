@@ -305,6 +305,45 @@ void prof_end(pmlg_ctx *ctx, cudaStream_t st)
     cudaEventRecord(ctx->prof.back().end, st);
 }
 
+int device_status(pmlg_ctx *ctx, cudaStream_t st)
+{
+    int h = 0;
+    PMLG_CUDA_TRY(cudaMemcpyAsync(&h, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (h) {
+        PMLG_CUDA_TRY(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), st));
+        PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+        set_error(ctx, "a bounded device wait gave up: the results of the calls since the last check are invalid");
+        return PMLG_ETIMEOUT;
+    }
+    return PMLG_OK;
+}
+
+// Waits on an mbarrier phase that nothing completes, for at most wait_ns, and
+// records the give-up in the error word exactly as the production kernels do:
+// the path by which a stuck wait reaches the host, exercised without a fault.
+__global__ void selftest_wait_kernel(int *err, unsigned long long wait_ns)
+{
+    __shared__ __align__(8) unsigned long long bar;
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(addr));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    __syncthreads();
+    unsigned long long t0;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+    unsigned done = 0;
+    for (int it = 0; it < (1 << 26) && !done; it++) {
+        asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\nselp.u32 %0, 1, 0, p;\n}"
+                     : "=r"(done) : "r"(addr) : "memory");
+        unsigned long long t;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+        if (t - t0 > wait_ns) break;
+    }
+    if (!done && threadIdx.x == 0) atomicExch(err, 1);
+}
+
 }  // namespace pmlg
 
 using namespace pmlg;
@@ -421,6 +460,24 @@ PMLG_API int pmlg_ctx_profile_read(pmlg_ctx *ctx, char *names, size_t names_len,
 PMLG_API const char *pmlg_ctx_last_error(const pmlg_ctx *ctx)
 {
     return ctx ? ctx->last_error : "null context";
+}
+
+PMLG_API int pmlg_ctx_device_status(pmlg_ctx *ctx, void *stream)
+{
+    if (!ctx) return PMLG_EINVAL;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    return pmlg::device_status(ctx, (cudaStream_t)stream);
+}
+
+PMLG_API int pmlg_ctx_selftest_timeout(pmlg_ctx *ctx, unsigned long long wait_ns, void *stream)
+{
+    if (!ctx || wait_ns == 0 || wait_ns > 1000000000ull) return PMLG_EINVAL;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    cudaStream_t st = (cudaStream_t)stream;
+    pmlg::selftest_wait_kernel<<<1, 32, 0, st>>>(ctx->d_err, wait_ns);
+    pmlg::count_launch(ctx);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    return pmlg::device_status(ctx, st);
 }
 
 PMLG_API const char *pmlg_strerror(int status)

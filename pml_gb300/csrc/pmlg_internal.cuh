@@ -161,6 +161,10 @@ namespace pmlg {
 
 void set_error(pmlg_ctx *ctx, const char *fmt, ...);
 
+// Waits for the stream, then reads and clears the device error word: PMLG_ETIMEOUT
+// when a bounded device wait of an earlier kernel on this context gave up.
+int device_status(pmlg_ctx *ctx, cudaStream_t st);
+
 // scalar host arithmetic
 uint64_t h_mulmod(uint64_t a, uint64_t b, uint64_t p);
 uint64_t h_powmod(uint64_t a, uint64_t e, uint64_t p);

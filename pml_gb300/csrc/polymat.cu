@@ -317,8 +317,7 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
     PMLG_TRY(h2d(ctx, dB, B, bB, st));
     PMLG_TRY(poly_mat_mul_device(ctx, dC, dA, dB, r, k, c, len1, len2, p, st));
     if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(C, dC, bC, cudaMemcpyDeviceToHost, st));
-    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
-    return PMLG_OK;
+    return device_status(ctx, st);
 }
 
 PMLG_API int pmlg_poly_mat_mulmid_host(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A,
@@ -341,7 +340,7 @@ PMLG_API int pmlg_poly_mat_mulmid_host(pmlg_ctx *ctx, uint64_t *res, const uint6
     PMLG_TRY(h2d(ctx, dB, B, bB, st));
     PMLG_TRY(poly_mat_mulmid_device(ctx, dC, dA, dB, r, k, c, len1, len2, nlo, nhi, p, st));
     if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(res, dC, bC, cudaMemcpyDeviceToHost, st));
-    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    PMLG_TRY(device_status(ctx, st));
     if (out_len) {
         // the actual max lengths are read on the host copies
         auto hostlen = [](const uint64_t *P, int64_t nent, int64_t len) {

@@ -1,0 +1,73 @@
+"""Failure detection and error reporting on the GPU.
+
+Every device-side wait of the kernels (mbarrier phases in the tensor-core
+pointwise form, published eliminations in the mbasis leaf) is bounded.  A wait
+that gives up sets the context's device error word and the kernel returns; the
+host reads the word (pmlg_ctx_device_status, and before every host-buffer or
+pmbasis call returns) and reports PMLG_ETIMEOUT, with the context still
+usable.  The test makes a wait run out on an mbarrier phase that nothing
+completes (no fault, no trap).  Invalid arguments return status codes where the
+reference has unchecked preconditions or aborts (nmod_poly_mat_multiply.h:34,45;
+verification.c:217)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import P998, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+EINVAL, EBADMOD, ETIMEOUT, EUNSUP = 1, 2, 6, 9
+
+
+def _stream():
+    import torch
+    return torch.cuda.current_stream().cuda_stream
+
+
+def test_bounded_wait_reaches_the_host(ctx):
+    import pml_gb300
+    st = ctx.lib.pmlg_ctx_selftest_timeout(ctx.handle, 2_000_000, _stream())
+    assert st == ETIMEOUT
+    assert b"bounded device wait" in ctx.lib.pmlg_ctx_last_error(ctx.handle)
+    # the word is cleared by the read, and the context still computes exactly
+    assert ctx.lib.pmlg_ctx_device_status(ctx.handle, _stream()) == 0
+    A = oracle.rand_poly_mat(3, 4, 20, P998, 1)
+    B = oracle.rand_poly_mat(4, 2, 17, P998, 2)
+    ctx.set_form(pml_gb300.FORM_F16_TC)
+    out = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), P998, ctx=ctx))
+    ctx.set_form(0)
+    assert np.array_equal(out, oracle.poly_mat_mul(A, B, P998))
+    assert ctx.lib.pmlg_ctx_device_status(ctx.handle, _stream()) == 0
+
+
+def test_selftest_limits(ctx):
+    assert ctx.lib.pmlg_ctx_selftest_timeout(ctx.handle, 0, _stream()) == EINVAL
+    assert ctx.lib.pmlg_ctx_selftest_timeout(ctx.handle, 2_000_000_000, _stream()) == EINVAL
+
+
+def test_status_codes_and_recovery(ctx):
+    import pml_gb300
+    from pml_gb300 import PmlgError
+    A = to_dev(oracle.rand_poly_mat(2, 2, 8, P998, 3))
+    with pytest.raises(PmlgError) as e:
+        pml_gb300.nmod_poly_mat_multiply(A, A, 1, ctx=ctx)
+    assert e.value.status == EBADMOD
+    F = to_dev(oracle.rand_poly_mat(4, 2, 16, P998, 4))
+    with pytest.raises(PmlgError) as e:
+        pml_gb300.nmod_poly_mat_pmbasis(F, 16, [0] * 4, P998 - 1, ctx=ctx)   # not a prime
+    assert e.value.status == EBADMOD
+    F65 = to_dev(oracle.rand_poly_mat(65, 2, 16, P998, 5))
+    with pytest.raises(PmlgError) as e:
+        pml_gb300.nmod_poly_mat_pmbasis(F65, 16, [0] * 65, P998, ctx=ctx)    # m > 64
+    assert e.value.status == EUNSUP
+    with pytest.raises(PmlgError) as e:
+        pml_gb300.nmod_poly_mat_mulmid(A, A, -1, 4, P998, ctx=ctx)
+    assert e.value.status == EINVAL
+    # nothing was left behind on the device, and a correct call follows
+    assert ctx.lib.pmlg_ctx_device_status(ctx.handle, _stream()) == 0
+    ab, sh = pml_gb300.nmod_poly_mat_pmbasis(F, 16, [0] * 4, P998, ctx=ctx)
+    ref, rsh = oracle.pmbasis(to_host(F), 16, [0] * 4, P998)
+    assert list(sh) == list(rsh) and np.array_equal(to_host(ab), ref)
