@@ -145,8 +145,11 @@ PMLG_API int pmlg_poly_mat_mulmid_host(pmlg_ctx *ctx, uint64_t *res, const uint6
                                        uint64_t p, int64_t *out_len, void *stream);
 
 /* A batch of independent products C_i = A_i * B_i with their own shapes,
- * lengths and moduli, computed together (one launch sequence for the whole
- * batch).  Device pointers.  Replaces a loop of nmod_poly_mat_multiply calls. */
+ * lengths and moduli, computed together.  Device pointers.  Replaces a loop of
+ * nmod_poly_mat_multiply calls.  Every job is validated and planned (CRT primes,
+ * NTT tables) before anything is launched; the jobs are then spread over the
+ * context's batch streams (largest first, onto the least loaded stream, each
+ * stream with its own scratch), forked from and joined back to `stream`. */
 typedef struct pmlg_polymat_job
 {
     int64_t r, k, c, len1, len2;

@@ -249,7 +249,9 @@ int make_plan(pmlg_ctx *ctx, uint64_t p, int lg, int64_t inner, int64_t minlen, 
         plan->ginv[j] = (j == 0) ? 1 : (uint32_t)h_invmod(pr, qj);
         plan->ginvq[j] = h_shoup_q(plan->ginv[j], qj);
         plan->qp[j] = plan->q[j] % p;
+        plan->qpq[j] = (uint64_t)(((unsigned __int128)plan->qp[j] << 64) / p);
     }
+    plan->onepq = (uint64_t)(((unsigned __int128)1 << 64) / p);
     return PMLG_OK;
 }
 
@@ -379,6 +381,11 @@ PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
     if (ctx->ws.ptr) cudaFree(ctx->ws.ptr);
     if (ctx->ws_aux.ptr) cudaFree(ctx->ws_aux.ptr);
     if (ctx->ws_pm.ptr) cudaFree(ctx->ws_pm.ptr);
+    if (ctx->ws_batch.ptr) cudaFree(ctx->ws_batch.ptr);
+    for (int i = 0; i < pmlg_ctx::kBatchStreams; i++)
+        if (ctx->bstream[i]) cudaStreamDestroy(ctx->bstream[i]);
+    for (int i = 0; i <= pmlg_ctx::kBatchStreams; i++)
+        if (ctx->bevent[i]) cudaEventDestroy(ctx->bevent[i]);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     for (auto &r : ctx->prof) { cudaEventDestroy(r.beg); cudaEventDestroy(r.end); }

@@ -344,10 +344,10 @@ ntt_inv_kernel(NttInvArgs a)
 __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int64_t nent, int64_t cnt,
                            uint64_t *__restrict__ out64, int64_t out_ld, int64_t out_cap)
 {
-    const int64_t total = nent * out_cap;
-    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e = idx / out_cap, d = idx - e * out_cap;
+    // entries along grid y, coefficients along x (no 64-bit division per element)
+    for (int64_t e = blockIdx.y; e < nent; e += gridDim.y)
+    for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < out_cap;
+         d += (int64_t)gridDim.x * blockDim.x) {
         if (d >= cnt) {
             out64[e * out_ld + d] = 0;
             continue;
@@ -370,9 +370,28 @@ __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int
             c[j] = cj >= qj ? cj - qj : cj;
         }
         const uint64_t p = plan.p;
-        unsigned __int128 x = c[plan.t - 1] % p;
-        for (int l = plan.t - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
-        out64[e * out_ld + d] = (uint64_t)x;
+        uint64_t res;
+        if (p <= (1ull << 63)) {
+            // Horner x <- x q_l + c_l mod p with 64-bit Shoup products (results in [0, 2p))
+            auto red = [&](uint64_t v) {   // v < 2^32 -> [0, p)
+                uint64_t r = v - __umul64hi(v, plan.onepq) * p;
+                return r >= p ? r - p : r;
+            };
+            uint64_t x = red(c[plan.t - 1]);
+            for (int l = plan.t - 2; l >= 0; l--) {
+                x = x * plan.qp[l] - __umul64hi(x, plan.qpq[l]) * p;
+                x = x >= p ? x - p : x;
+                const uint64_t cl = red(c[l]);
+                const uint64_t s = x + cl;
+                x = (s < x || s >= p) ? s - p : s;
+            }
+            res = x;
+        } else {
+            unsigned __int128 x = c[plan.t - 1] % p;
+            for (int l = plan.t - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
+            res = (uint64_t)x;
+        }
+        out64[e * out_ld + d] = res;
     }
 }
 
@@ -465,13 +484,13 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st)
 int crt_combine(pmlg_ctx *ctx, const CrtPlan &plan, const uint32_t *res32, int64_t nent, int64_t cnt,
                 uint64_t *out64, int64_t out_ld, int64_t out_cap, cudaStream_t st)
 {
-    const int64_t total = nent * out_cap;
-    if (total <= 0) return PMLG_OK;
-    int64_t blocks = (total + 255) / 256;
-    const int64_t cap = (int64_t)ctx->sm_count * 16;
-    if (blocks > cap) blocks = cap;
+    if (nent <= 0 || out_cap <= 0) return PMLG_OK;
+    const int64_t by = nent < 65535 ? nent : 65535;
+    int64_t bx = (out_cap + 255) / 256;
+    const int64_t cap = ((int64_t)ctx->sm_count * 16 + by - 1) / by;   // about 16 CTAs per SM in all
+    if (bx > cap) bx = cap;
     prof_begin(ctx, "crt", st);
-    crt_kernel<<<(unsigned)blocks, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap);
+    crt_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap);
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());

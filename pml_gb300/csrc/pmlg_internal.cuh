@@ -93,8 +93,10 @@ struct CrtPlan
     uint32_t qmod[kMaxPrimes][kMaxPrimes];
     uint32_t qmodq[kMaxPrimes][kMaxPrimes];
     uint32_t ginv[kMaxPrimes], ginvq[kMaxPrimes];
-    // for the final Horner mod p: q_l mod p (64-bit)
-    uint64_t qp[kMaxPrimes];
+    // for the final Horner mod p: q_l mod p and its 64-bit Shoup quotient
+    // floor(qp * 2^64 / p), and floor(2^64 / p) to reduce residues below 2^30
+    uint64_t qp[kMaxPrimes], qpq[kMaxPrimes];
+    uint64_t onepq;
     uint64_t p;
 };
 
@@ -130,8 +132,13 @@ struct pmlg_ctx
     size_t pinned_bytes = 0;
     unsigned long long launches = 0;   // kernels launched through this context
     int *d_err = nullptr;              // device error word: a bounded wait gave up
+    // streams and events of the batched products (created on first use)
+    static constexpr int kBatchStreams = 8;
+    cudaStream_t bstream[kBatchStreams] = {};
+    cudaEvent_t bevent[kBatchStreams + 1] = {};
+    pmlg::Workspace ws_batch;      // per-stream scratch of the batched products
     // cached NTT tables
-    static constexpr int kMaxTables = 64;
+    static constexpr int kMaxTables = 256;
     pmlg::NttTable tables[kMaxTables];
     int ntables = 0;
     char last_error[256] = {0};

@@ -12,7 +12,9 @@
 #include "ntt.cuh"
 #include "pointwise.cuh"
 
+#include <algorithm>
 #include <cstring>
+#include <vector>
 
 namespace pmlg {
 
@@ -365,10 +367,90 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
     if (!ctx || (njobs > 0 && !jobs) || njobs < 0) return PMLG_EINVAL;
     cudaStream_t st = (cudaStream_t)stream;
     PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    // 1. validate every job, build its transform plan and tables (host work, before any launch)
+    struct Item
+    {
+        ProductJob j;
+        CrtPlan plan;
+        size_t scratch;
+        double work;
+    };
+    std::vector<Item> items;
+    items.reserve((size_t)njobs);
     for (int64_t i = 0; i < njobs; i++) {
         const pmlg_polymat_job &J = jobs[i];
         PMLG_TRY(check_common(ctx, J.C, J.A, J.B, J.r, J.k, J.c, J.len1, J.len2, J.p));
-        PMLG_TRY(poly_mat_mul_device(ctx, J.C, J.A, J.B, J.r, J.k, J.c, J.len1, J.len2, J.p, st));
+        const int64_t clen = (J.len1 > 0 && J.len2 > 0) ? J.len1 + J.len2 - 1 : 0;
+        if (J.r == 0 || J.c == 0 || clen == 0) continue;
+        if (J.k == 0) {
+            PMLG_CUDA_TRY(cudaMemsetAsync(J.C, 0, (size_t)(J.r * J.c * clen) * 8, st));
+            continue;
+        }
+        Item it{};
+        ProductJob &j = it.j;
+        j.r = J.r; j.k = J.k; j.c = J.c;
+        j.A = J.A; j.lda = J.len1; j.a_off = 0; j.a_len = J.len1;
+        j.B = J.B; j.ldb = J.len2; j.b_off = 0; j.b_len = J.len2;
+        j.C = J.C; j.ldc = clen; j.c_cap = clen;
+        j.lo = 0; j.cnt = clen;
+        j.lg = lg_for(clen);
+        j.p = J.p;
+        if (j.lg > kMaxLgN) {
+            set_error(ctx, "job %lld: product length %lld needs a transform beyond 2^%d", (long long)i,
+                      (long long)clen, kMaxLgN);
+            return PMLG_ELEN;
+        }
+        const int64_t minlen = j.a_len < j.b_len ? j.a_len : j.b_len;
+        PMLG_TRY(make_plan(ctx, j.p, j.lg, j.k, minlen, &it.plan));
+        for (int q = 0; q < it.plan.t; q++) {
+            const NttTable *tab;
+            PMLG_TRY(get_table(ctx, it.plan.q[q], j.lg, &tab));
+        }
+        it.scratch = (product_scratch_bytes(j, it.plan) + 255) & ~(size_t)255;
+        const double N = (double)(1ll << j.lg);
+        it.work = it.plan.t * N * ((double)(j.r * j.k + j.k * j.c + j.r * j.c) * j.lg + (double)j.r * j.k * j.c);
+        items.push_back(it);
+    }
+    if (items.empty()) return PMLG_OK;
+    // 2. spread the jobs over the batch streams, largest first onto the least loaded stream;
+    //    each stream owns a scratch region as large as its largest job
+    const int K = (int)(items.size() < (size_t)pmlg_ctx::kBatchStreams ? items.size() : pmlg_ctx::kBatchStreams);
+    std::vector<int> order(items.size());
+    for (size_t i = 0; i < items.size(); i++) order[i] = (int)i;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return items[a].work > items[b].work; });
+    std::vector<int> slot(items.size());
+    std::vector<double> load(K, 0.0);
+    std::vector<size_t> need(K, 0);
+    for (int idx : order) {
+        int s = 0;
+        for (int t = 1; t < K; t++)
+            if (load[t] < load[s]) s = t;
+        slot[idx] = s;
+        load[s] += items[idx].work;
+        if (items[idx].scratch > need[s]) need[s] = items[idx].scratch;
+    }
+    std::vector<size_t> off(K, 0);
+    size_t total = 0;
+    for (int s = 0; s < K; s++) {
+        off[s] = total;
+        total += need[s];
+    }
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws_batch, total));
+    for (int s = 0; s < K; s++)
+        if (!ctx->bstream[s]) PMLG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->bstream[s], cudaStreamNonBlocking));
+    for (int s = 0; s <= K; s++)
+        if (!ctx->bevent[s]) PMLG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->bevent[s], cudaEventDisableTiming));
+    // 3. fork from the caller's stream, run, join back
+    PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[K], st));
+    for (int s = 0; s < K; s++) PMLG_CUDA_TRY(cudaStreamWaitEvent(ctx->bstream[s], ctx->bevent[K], 0));
+    char *base = (char *)ctx->ws_batch.ptr;
+    for (int idx : order) {
+        const int s = slot[idx];
+        PMLG_TRY(product_run(ctx, items[idx].j, items[idx].plan, base + off[s], ctx->form, ctx->bstream[s]));
+    }
+    for (int s = 0; s < K; s++) {
+        PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[s], ctx->bstream[s]));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ctx->bevent[s], 0));
     }
     return PMLG_OK;
 }
