@@ -5,10 +5,13 @@ Headline workload: nmod_poly_mat_mul of two 64x64 polynomial matrices, every
 entry of length 4096 (degree < 4096), p = 998244353, coefficients uniform in
 [0, p) from a seed (uint64 storage): forward NTT of length 8192, 8192 pointwise
 64x64x64 products mod p, inverse NTT.  One "step" = one full product.
-`value` is the time of one product with the split-limb INT8 tensor-core form,
-inputs resident in HBM (267 MB of inputs, larger than L2, so no flush is
-needed); the same product with the CUDA-core form is reported beside it, and
-pmbasis of a 64x32 matrix at order 8192 (zero shift) for both forms.
+`value` is the time of one product with the tensor-core form (FP16 digits on
+tcgen05: GB300 has no tcgen05 INT8 kind), inputs resident in HBM (268 MB of
+inputs, larger than L2, so no flush is needed).  The INT8 split-limb form
+(mma.sync) and the CUDA-core form of the same pipeline are timed beside it;
+also reported: pmbasis of a 64x32 matrix at order 8192 (zero shift), the
+pointwise contraction alone (4096 batched 64x64 products) and 256 batched
+uneven products, each for every form.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl pml|reference]
 
