@@ -38,42 +38,60 @@ size_t product_scratch_bytes(const ProductJob &j, const CrtPlan &plan)
     return b;
 }
 
-int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch, int form,
-                cudaStream_t st)
+// The scratch of a product: evaluations of A, B and C per prime (point-tiled),
+// and the CRT residues when p is not the NTT prime.
+struct ProductBufs
+{
+    uint32_t *EA, *EB, *EC, *R32;
+    const NttTable *tabs[kMaxPrimes];
+};
+
+static int product_bufs(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch, ProductBufs &b)
 {
     const int64_t N = 1ll << j.lg;
     const int t = plan.t;
-    const int64_t nA = j.r * j.k, nB = j.k * j.c, nC = j.r * j.c;
     char *w = (char *)scratch;
-    uint32_t *EA = (uint32_t *)w; w += align256((size_t)t * N * nA * 4);
-    uint32_t *EB = (uint32_t *)w; w += align256((size_t)t * N * nB * 4);
-    uint32_t *EC = (uint32_t *)w; w += align256((size_t)t * N * nC * 4);
-    uint32_t *R32 = plan.direct ? nullptr : (uint32_t *)w;
+    b.EA = (uint32_t *)w; w += align256((size_t)t * N * j.r * j.k * 4);
+    b.EB = (uint32_t *)w; w += align256((size_t)t * N * j.k * j.c * 4);
+    b.EC = (uint32_t *)w; w += align256((size_t)t * N * j.r * j.c * 4);
+    b.R32 = plan.direct ? nullptr : (uint32_t *)w;
+    for (int i = 0; i < t; i++) PMLG_TRY(get_table(ctx, plan.q[i], j.lg, &b.tabs[i]));
+    return PMLG_OK;
+}
 
-    const NttTable *tabs[kMaxPrimes];
-    for (int i = 0; i < t; i++) PMLG_TRY(get_table(ctx, plan.q[i], j.lg, &tabs[i]));
-
+// forward transforms of A (which = 0) or B (which = 1)
+static int product_forward(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, const ProductBufs &b,
+                           int which, cudaStream_t st)
+{
+    const int64_t N = 1ll << j.lg;
     NttFwdArgs fa{};
     fa.lg = j.lg;
-    fa.t = t;
+    fa.t = plan.t;
     fa.reduce = !plan.direct;
-    for (int i = 0; i < t; i++)
-        fa.tab[i] = ntt_dev(tabs[i], false);
-    // A
-    fa.in = j.A; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = nA;
-    fa.out = EA; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
-    PMLG_TRY(ntt_forward(ctx, fa, st));
-    // B
-    fa.in = j.B; fa.in_ld = j.ldb; fa.in_off = j.b_off; fa.L = j.b_len; fa.nent = nB;
-    fa.out = EB; fa.prime_stride = N * nB; fa.tile_stride = kPtTile * nB;
-    PMLG_TRY(ntt_forward(ctx, fa, st));
+    for (int i = 0; i < plan.t; i++) fa.tab[i] = ntt_dev(b.tabs[i], false);
+    if (which == 0) {
+        const int64_t nA = j.r * j.k;
+        fa.in = j.A; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = nA;
+        fa.out = b.EA; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
+    } else {
+        const int64_t nB = j.k * j.c;
+        fa.in = j.B; fa.in_ld = j.ldb; fa.in_off = j.b_off; fa.L = j.b_len; fa.nent = nB;
+        fa.out = b.EB; fa.prime_stride = N * nB; fa.tile_stride = kPtTile * nB;
+    }
+    return ntt_forward(ctx, fa, st);
+}
 
-    // pointwise products, one prime at a time
-    for (int i = 0; i < t; i++) {
+// pointwise products, one prime at a time (scaled by 1/N for the inverse transform)
+static int product_pointwise(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, const ProductBufs &b,
+                             int form, cudaStream_t st)
+{
+    const int64_t N = 1ll << j.lg;
+    const int64_t nA = j.r * j.k, nB = j.k * j.c, nC = j.r * j.c;
+    for (int i = 0; i < plan.t; i++) {
         PwArgs pa{};
-        pa.A = {EA + (size_t)i * N * nA, kPtTile * nA, j.k};
-        pa.B = {EB + (size_t)i * N * nB, kPtTile * nB, j.c};
-        pa.C = EC + (size_t)i * N * nC;
+        pa.A = {b.EA + (size_t)i * N * nA, kPtTile * nA, j.k};
+        pa.B = {b.EB + (size_t)i * N * nB, kPtTile * nB, j.c};
+        pa.C = b.EC + (size_t)i * N * nC;
         pa.s_tile_c = kPtTile * nC;
         pa.ldc = j.c;
         pa.pt_tile = kPtTile;
@@ -81,21 +99,41 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
         pa.s_p = 1;
         pa.npts = N;
         pa.accumulate = 0;
-        pointwise_set_modulus(pa, plan.q[i], tabs[i]->ninv);   // the 1/N of the inverse transform
+        pointwise_set_modulus(pa, plan.q[i], b.tabs[i]->ninv);   // the 1/N of the inverse transform
         PMLG_TRY(pointwise_blocked(ctx, pa, j.r, j.k, j.c, form, st));
     }
-
-    NttInvArgs ia{};
-    ia.in = EC; ia.prime_stride = N * nC; ia.tile_stride = kPtTile * nC; ia.nent = nC;
-    ia.lo = j.lo; ia.cnt = j.cnt;
-    ia.out64 = j.C; ia.out_ld = j.ldc; ia.out_cap = j.c_cap;
-    ia.res32 = R32;
-    ia.lg = j.lg; ia.t = t; ia.direct = plan.direct;
-    for (int i = 0; i < t; i++)
-        ia.tab[i] = ntt_dev(tabs[i], true);
-    PMLG_TRY(ntt_inverse(ctx, ia, st));
-    if (!plan.direct) PMLG_TRY(crt_combine(ctx, plan, R32, nC, j.cnt, j.C, j.ldc, j.c_cap, st));
     return PMLG_OK;
+}
+
+// inverse transforms of the output entries [e0, e1) (+ CRT when p is not the NTT prime)
+static int product_inverse(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, const ProductBufs &b,
+                           int64_t e0, int64_t e1, cudaStream_t st)
+{
+    const int64_t N = 1ll << j.lg;
+    const int64_t nC = j.r * j.c, ne = e1 - e0;
+    if (ne <= 0) return PMLG_OK;
+    NttInvArgs ia{};
+    ia.in = b.EC + e0 * kPtTile; ia.prime_stride = N * nC; ia.tile_stride = kPtTile * nC; ia.nent = ne;
+    ia.lo = j.lo; ia.cnt = j.cnt;
+    ia.out64 = j.C + e0 * j.ldc; ia.out_ld = j.ldc; ia.out_cap = j.c_cap;
+    ia.res32 = b.R32;
+    ia.lg = j.lg; ia.t = plan.t; ia.direct = plan.direct;
+    for (int i = 0; i < plan.t; i++) ia.tab[i] = ntt_dev(b.tabs[i], true);
+    PMLG_TRY(ntt_inverse(ctx, ia, st));
+    if (!plan.direct)
+        PMLG_TRY(crt_combine(ctx, plan, b.R32, ne, j.cnt, j.C + e0 * j.ldc, j.ldc, j.c_cap, st));
+    return PMLG_OK;
+}
+
+int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch, int form,
+                cudaStream_t st)
+{
+    ProductBufs b;
+    PMLG_TRY(product_bufs(ctx, j, plan, scratch, b));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 0, st));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 1, st));
+    PMLG_TRY(product_pointwise(ctx, j, plan, b, form, st));
+    return product_inverse(ctx, j, plan, b, 0, j.r * j.c, st);
 }
 
 int mulmid_prepare(ProductJob &j, int64_t len1, int64_t len2, int64_t nlo, int64_t nhi)
@@ -184,6 +222,31 @@ static int run_job_alloc(pmlg_ctx *ctx, const ProductJob &j, cudaStream_t st)
     return product_run(ctx, j, plan, ctx->ws.ptr, ctx->form, st);
 }
 
+// the job of a full product C = A * B with coefficient-contiguous entries
+static void full_product_job(ProductJob &j, uint64_t *C, const uint64_t *A, const uint64_t *B, int64_t r,
+                             int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p)
+{
+    const int64_t clen = len1 + len2 - 1;
+    j = ProductJob{};
+    j.r = r; j.k = k; j.c = c;
+    j.A = A; j.lda = len1; j.a_off = 0; j.a_len = len1;
+    j.B = B; j.ldb = len2; j.b_off = 0; j.b_len = len2;
+    j.C = C; j.ldc = clen; j.c_cap = clen;
+    j.lo = 0; j.cnt = clen;
+    j.lg = lg_for(clen);
+    j.p = p;
+}
+
+// the context's side streams and events (batched products, host-buffer pipelining)
+static int ensure_side_streams(pmlg_ctx *ctx, int nstreams)
+{
+    for (int s = 0; s < nstreams; s++)
+        if (!ctx->bstream[s]) PMLG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->bstream[s], cudaStreamNonBlocking));
+    for (int s = 0; s <= pmlg_ctx::kBatchStreams; s++)
+        if (!ctx->bevent[s]) PMLG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->bevent[s], cudaEventDisableTiming));
+    return PMLG_OK;
+}
+
 int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B, int64_t r,
                         int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p, cudaStream_t st)
 {
@@ -193,14 +256,8 @@ int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uin
         PMLG_CUDA_TRY(cudaMemsetAsync(C, 0, (size_t)(r * c * clen) * 8, st));
         return PMLG_OK;
     }
-    ProductJob j{};
-    j.r = r; j.k = k; j.c = c;
-    j.A = A; j.lda = len1; j.a_off = 0; j.a_len = len1;
-    j.B = B; j.ldb = len2; j.b_off = 0; j.b_len = len2;
-    j.C = C; j.ldc = clen; j.c_cap = clen;
-    j.lo = 0; j.cnt = clen;
-    j.lg = lg_for(clen);
-    j.p = p;
+    ProductJob j;
+    full_product_job(j, C, A, B, r, k, c, len1, len2, p);
     if (j.lg > kMaxLgN) {
         set_error(ctx, "product length %lld needs a transform beyond 2^%d", (long long)clen, kMaxLgN);
         return PMLG_ELEN;
@@ -315,10 +372,51 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
     PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, oC + bC + 256));
     char *base = (char *)ctx->ws_aux.ptr;
     uint64_t *dA = (uint64_t *)(base + oA), *dB = (uint64_t *)(base + oB), *dC = (uint64_t *)(base + oC);
+    if (r == 0 || c == 0 || clen == 0 || k == 0) {
+        PMLG_TRY(h2d(ctx, dA, A, bA, st));
+        PMLG_TRY(h2d(ctx, dB, B, bB, st));
+        PMLG_TRY(poly_mat_mul_device(ctx, dC, dA, dB, r, k, c, len1, len2, p, st));
+        if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(C, dC, bC, cudaMemcpyDeviceToHost, st));
+        return device_status(ctx, st);
+    }
+    ProductJob j;
+    full_product_job(j, dC, dA, dB, r, k, c, len1, len2, p);
+    if (j.lg > kMaxLgN) {
+        set_error(ctx, "product length %lld needs a transform beyond 2^%d", (long long)clen, kMaxLgN);
+        return PMLG_ELEN;
+    }
+    CrtPlan plan;
+    PMLG_TRY(make_plan(ctx, p, j.lg, k, len1 < len2 ? len1 : len2, &plan));
+    PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan)));
+    ProductBufs b;
+    PMLG_TRY(product_bufs(ctx, j, plan, ctx->ws.ptr, b));
+    PMLG_TRY(ensure_side_streams(ctx, 1));
+    // Copies overlap the transforms: B is copied (side stream) while A is
+    // transformed, and C goes back in entry chunks while the later chunks
+    // are still being transformed back.
+    cudaStream_t cs = ctx->bstream[0];
+    cudaEvent_t *ev = ctx->bevent;
+    PMLG_CUDA_TRY(cudaEventRecord(ev[0], st));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[0], 0));
     PMLG_TRY(h2d(ctx, dA, A, bA, st));
-    PMLG_TRY(h2d(ctx, dB, B, bB, st));
-    PMLG_TRY(poly_mat_mul_device(ctx, dC, dA, dB, r, k, c, len1, len2, p, st));
-    if (bC) PMLG_CUDA_TRY(cudaMemcpyAsync(C, dC, bC, cudaMemcpyDeviceToHost, st));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 0, st));
+    PMLG_TRY(h2d(ctx, dB, B, bB, cs));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 1, cs));
+    PMLG_CUDA_TRY(cudaEventRecord(ev[1], cs));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ev[1], 0));
+    PMLG_TRY(product_pointwise(ctx, j, plan, b, ctx->form, st));
+    const int64_t nC = r * c;
+    const int nchunk = plan.direct && nC >= 4 ? 4 : 1;
+    for (int i = 0; i < nchunk; i++) {
+        const int64_t e0 = nC * i / nchunk, e1 = nC * (i + 1) / nchunk;
+        PMLG_TRY(product_inverse(ctx, j, plan, b, e0, e1, st));
+        PMLG_CUDA_TRY(cudaEventRecord(ev[2 + i], st));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[2 + i], 0));
+        PMLG_CUDA_TRY(cudaMemcpyAsync(C + e0 * clen, dC + e0 * clen, (size_t)((e1 - e0) * clen) * 8,
+                                      cudaMemcpyDeviceToHost, cs));
+    }
+    PMLG_CUDA_TRY(cudaEventRecord(ev[6], cs));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ev[6], 0));
     return device_status(ctx, st);
 }
 
@@ -388,13 +486,7 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
         }
         Item it{};
         ProductJob &j = it.j;
-        j.r = J.r; j.k = J.k; j.c = J.c;
-        j.A = J.A; j.lda = J.len1; j.a_off = 0; j.a_len = J.len1;
-        j.B = J.B; j.ldb = J.len2; j.b_off = 0; j.b_len = J.len2;
-        j.C = J.C; j.ldc = clen; j.c_cap = clen;
-        j.lo = 0; j.cnt = clen;
-        j.lg = lg_for(clen);
-        j.p = J.p;
+        full_product_job(j, J.C, J.A, J.B, J.r, J.k, J.c, J.len1, J.len2, J.p);
         if (j.lg > kMaxLgN) {
             set_error(ctx, "job %lld: product length %lld needs a transform beyond 2^%d", (long long)i,
                       (long long)clen, kMaxLgN);
@@ -436,10 +528,7 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
         total += need[s];
     }
     PMLG_TRY(ws_reserve(ctx, &ctx->ws_batch, total));
-    for (int s = 0; s < K; s++)
-        if (!ctx->bstream[s]) PMLG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->bstream[s], cudaStreamNonBlocking));
-    for (int s = 0; s <= K; s++)
-        if (!ctx->bevent[s]) PMLG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->bevent[s], cudaEventDisableTiming));
+    PMLG_TRY(ensure_side_streams(ctx, K));
     // 3. fork from the caller's stream, run, join back
     PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[K], st));
     for (int s = 0; s < K; s++) PMLG_CUDA_TRY(cudaStreamWaitEvent(ctx->bstream[s], ctx->bevent[K], 0));
