@@ -31,6 +31,7 @@ struct PwArgs
     uint32_t wd[4][3];  // scale * 2^(8i + 10j) mod q for the FP16-digit recombination
     uint64_t negoff;    // multiple of q >= 2^56, makes signed digit sums non-negative
     int accumulate;     // C += A*B instead of C = A*B
+    int lmt;            // FP16 form: blocks of 2^lmt >= r, k, c; 64 >> lmt points share one MMA problem
     int *err;           // device error word (bounded waits that gave up), may be null
 };
 
