@@ -56,9 +56,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the pointwise-batch and batched-uneven measurements")
-    ap.add_argument("--profile-case", choices=["product", "pmbasis"], default=None,
-                    help="run one product per form (or one pmbasis at order 1024) and exit: "
-                         "the small case for kernel captures")
+    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven"], default=None,
+                    help="run one product per form (or one pmbasis at order 1024, one 4096-product "
+                         "pointwise batch per form, one batched-uneven call with the FP16 form) and exit: "
+                         "the small cases for kernel captures")
     return ap.parse_args()
 
 
@@ -80,6 +81,16 @@ def run_profile_case(args):
         print(json.dumps({"profile_case": "product",
                           "forms_agree": all(bool(torch.equal(outs[0], o)) for o in outs),
                           "launches": ctx.launches}))
+    elif args.profile_case == "pwbatch":
+        forms = (("f16_tc", pml_gb300.FORM_F16_TC), ("int8_tc", pml_gb300.FORM_INT8_TC),
+                 ("cuda_core", pml_gb300.FORM_CUDA_CORE))
+        r = measure_pointwise_batch(ctx, torch.device("cuda", 0), torch.cuda.current_stream(), forms, 0)
+        print(json.dumps({"profile_case": "pwbatch", "forms_agree": r["forms_agree"], "launches": ctx.launches}))
+    elif args.profile_case == "uneven":
+        ctx.set_form(pml_gb300.FORM_F16_TC)
+        r = measure_batched_uneven(ctx, torch.device("cuda", 0), torch.cuda.current_stream(),
+                                   (("f16_tc", pml_gb300.FORM_F16_TC),), 0)
+        print(json.dumps({"profile_case": "uneven", "ms": r["f16_tc_ms"], "launches": ctx.launches}))
     else:
         rng = np.random.default_rng(7)
         F = rng.integers(0, P, size=(PM_M, PM_N, 1024), dtype=np.uint64)
@@ -305,7 +316,8 @@ def measure_pointwise_batch(ctx, dev, st, forms, rank):
         res[name + "_ms"] = ms
         res[name + "_gmac_per_s"] = nb * 64 ** 3 / ms / 1e6
         outs[name] = out
-    res["forms_agree"] = all(bool(torch.equal(outs["cuda_core"], o)) for o in outs.values())
+    ref = outs.get("cuda_core", next(iter(outs.values())))
+    res["forms_agree"] = all(bool(torch.equal(ref, o)) for o in outs.values())
     res["config"] = "4096 products 64x64 . 64x64 mod 998244353, uint32 entries uniform in [0, p), batch-major"
     return res
 
@@ -331,8 +343,8 @@ def measure_batched_uneven(ctx, dev, st, forms, rank):
         ms, out = _time_calls(lambda: pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx), st, 3, 1)
         res[name + "_ms"] = ms
         outs[name] = out
-    res["forms_agree"] = all(all(bool(torch.equal(a, b)) for a, b in zip(outs["cuda_core"], o))
-                             for o in outs.values())
+    ref = outs.get("cuda_core", next(iter(outs.values())))
+    res["forms_agree"] = all(all(bool(torch.equal(a, b)) for a, b in zip(ref, o)) for o in outs.values())
     res["config"] = ("256 instances, m uniform in {4..48}, length 2^U(6,12), half p = 998244353, "
                      "half seeded 59-bit primes (CRT over NTT primes), uniform coefficients")
     res["coefficient_macs"] = macs
