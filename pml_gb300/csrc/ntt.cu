@@ -20,6 +20,30 @@ namespace pmlg {
 
 __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 
+// Cache policy: coefficients and evaluations stream through once and are not
+// kept in L1 (no_allocate); the group twiddle tables are kept (evict_last).
+__device__ __forceinline__ uint64_t ld_stream(const uint64_t *p)
+{
+    uint64_t v;
+    asm("ld.global.nc.L1::no_allocate.u64 %0, [%1];" : "=l"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint4 ld_stream(const uint4 *p)
+{
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint2 ld_keep(const uint2 *p)
+{
+    uint2 v;
+    asm("ld.global.nc.L1::evict_last.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
 __device__ __forceinline__ uint32_t csub(uint32_t x, uint32_t m) { return min(x, x - m); }
 
 // Radix-2^G decimation-in-frequency butterflies on each of the 16 >> G
@@ -97,7 +121,7 @@ __device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &
     const uint2 *g = T.w + 15 * ((1 << lls) - 1) + off;
 #pragma unroll
     for (int m = 1; m < 16; m++) {
-        const uint2 tw = __ldg(&g[(m - 1) << lls]);
+        const uint2 tw = ld_keep(&g[(m - 1) << lls]);
         v[m] = shoup_mul(v[m], tw.x, tw.y, T.q);
     }
 }
@@ -239,7 +263,7 @@ __device__ __forceinline__ void fwd_transform(uint32_t (&v)[16], uint32_t *x, in
         const int d = t + m * TPT;
         uint32_t val = 0;
         if (d < L) {
-            const uint64_t s = src[d];
+            const uint64_t s = ld_stream(src + d);
             val = a.reduce ? mod64_q(s, T.q, T.r32, T.r32q, T.oneq) : (uint32_t)s;
         }
         v[m] = val;
@@ -275,7 +299,8 @@ ntt_fwd_kernel(NttFwdArgs a)
             uint4 o;
             o.x = csub(v[4 * c + 0], q); o.y = csub(v[4 * c + 1], q);
             o.z = csub(v[4 * c + 2], q); o.w = csub(v[4 * c + 3], q);
-            *reinterpret_cast<uint4 *>(dst + (int64_t)(4 * t + c) * a.tile_stride) = o;
+            const int pt = 16 * t + 4 * c;   // first of the four points
+            *reinterpret_cast<uint4 *>(dst + (int64_t)(pt / kPtTile) * a.tile_stride + pt % kPtTile) = o;
         }
     }
 }
@@ -299,7 +324,9 @@ ntt_inv_kernel(NttInvArgs a)
         const uint32_t *src = a.in + j * a.prime_stride + e * kPtTile;
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            const uint4 o = *reinterpret_cast<const uint4 *>(src + (int64_t)(4 * t + c) * a.tile_stride);
+            const int pt = 16 * t + 4 * c;
+            const uint4 o = ld_stream(reinterpret_cast<const uint4 *>(src + (int64_t)(pt / kPtTile) * a.tile_stride +
+                                                                     pt % kPtTile));
             v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
         }
     } else {

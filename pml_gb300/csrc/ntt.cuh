@@ -30,11 +30,18 @@ inline NttDev ntt_dev(const NttTable *t, bool inverse)
 }
 
 // Evaluations are stored "point-tiled": for prime j, point t and matrix entry e,
-//   E[j * prime_stride + (t / 4) * tile_stride + e * 4 + (t % 4)],
-// tile_stride = 4 * (number of entries), so that the four consecutive points
-// of one entry are one 16-byte word and all entries of a 4-point tile are
-// contiguous.  Point t holds the evaluation at w^bitrev(t).
-constexpr int kPtTile = 4;
+//   E[j * prime_stride + (t / T) * tile_stride + e * T + (t % T)],  T = kPtTile,
+// tile_stride = T * (number of entries), so that the T consecutive points of
+// one entry are one 16-byte word (T = 4) and all entries of a tile are
+// contiguous.  Point t holds the evaluation at w^bitrev(t).  The pointwise
+// kernels read two points of an entry in one 8-byte load.  Measured on GB300
+// for the 64x64 product at length 4096: T = 8 made the forward NTT 5 us faster
+// and the pointwise products 27 us slower; T = 16 is worse still.
+#ifndef PMLG_PT_TILE
+#define PMLG_PT_TILE 4
+#endif
+constexpr int kPtTile = PMLG_PT_TILE;
+static_assert(kPtTile == 4 || kPtTile == 8 || kPtTile == 16, "point tile");
 
 struct NttFwdArgs
 {

@@ -12,6 +12,7 @@
 //    as sum_s S_s * (2^(8s) mod q) < 2^57 and reduced mod q on the CUDA cores.
 //    (tcgen05 kind::i8 does not exist on sm_103a; mma.sync is the INT8 path.)
 #include "pointwise.cuh"
+#include "ntt.cuh"
 
 #include <cuda_fp16.h>
 
@@ -425,7 +426,8 @@ __device__ __forceinline__ uint2 f16_load_pair(const PwOperand &op, int64_t e, i
                                                const PwArgs &a)
 {
     if (TILE)   // point-tiled layout, pt0 even: the two values are adjacent
-        return __ldg(reinterpret_cast<const uint2 *>(op.base + ((pt0 >> 2) * op.s_tile + e * 4 + (pt0 & 3))));
+        return __ldg(reinterpret_cast<const uint2 *>(op.base + ((pt0 / kPtTile) * op.s_tile + e * kPtTile +
+                                                                (pt0 % kPtTile))));
     uint2 v;
     v.x = op.base[pw_off(pt0, e, lg, op.s_tile, a.s_e, a.s_p)];
     v.y = has1 ? op.base[pw_off(pt0 + 1, e, lg, op.s_tile, a.s_e, a.s_p)] : 0u;
@@ -649,7 +651,8 @@ pw_f16_kernel(PwArgs a)
                 v1 = v1 >= q ? v1 - q : v1;
                 const int64_t ce = (int64_t)ii * a.ldc + n;
                 if (TILE) {
-                    uint2 *dst = reinterpret_cast<uint2 *>(a.C + ((pt0 >> 2) * a.s_tile_c + ce * 4 + (pt0 & 3)));
+                    uint2 *dst = reinterpret_cast<uint2 *>(a.C + ((pt0 / kPtTile) * a.s_tile_c + ce * kPtTile +
+                                                                  (pt0 % kPtTile)));
                     if (a.accumulate) {
                         const uint2 old = *dst;
                         v0 += old.x;
@@ -740,7 +743,7 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
         PwArgs b = a;
         b.err = ctx->d_err;
         // point pairs share 8 aligned bytes in the point-tiled layout
-        const bool tile = a.pt_tile == 4 && a.s_e == 4 && a.s_p == 1 && (a.npts & 1) == 0 &&
+        const bool tile = a.pt_tile == kPtTile && a.s_e == kPtTile && a.s_p == 1 && (a.npts & 1) == 0 &&
                           ((uintptr_t)a.A.base & 7) == 0 && ((uintptr_t)a.B.base & 7) == 0 &&
                           ((uintptr_t)a.C & 7) == 0 && (a.A.s_tile & 1) == 0 && (a.B.s_tile & 1) == 0 &&
                           (a.s_tile_c & 1) == 0;
