@@ -236,6 +236,9 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
 #ifndef PMLG_NTT_INV_REGS
 #define PMLG_NTT_INV_REGS 40
 #endif
+#ifndef PMLG_NTT_INV_PERSIST
+#define PMLG_NTT_INV_PERSIST 1   // persistent, prefetching inverse kernel for N >= 4096
+#endif
 
 // threads of a CTA: one transform of N/16 threads, at least 256
 template <int LG>
@@ -247,6 +250,8 @@ struct NttBlock
     // resident CTAs the kernels ask registers for (per-thread register budgets above)
     static constexpr int FWD_MIN = min_ctas(PMLG_NTT_FWD_REGS);
     static constexpr int INV_MIN = min_ctas(PMLG_NTT_INV_REGS);
+    // persistent inverse: shared memory (transform + prefetch) allows 6 / 3 / 1 CTAs
+    static constexpr int INVP_MIN = LG <= 12 ? 6 : LG == 13 ? 3 : 1;
 };
 
 // Loads the first group (elements t + m N/16) and runs all groups; with ZH the
@@ -305,6 +310,42 @@ ntt_fwd_kernel(NttFwdArgs a)
     }
 }
 
+// Output of an inverse transform: element m of thread t is coefficient t + m N/16.
+template <int LG>
+__device__ __forceinline__ void inv_store(const uint32_t (&v)[16], const NttInvArgs &a, int64_t e, int j, int t,
+                                          uint32_t q)
+{
+    constexpr int TPT = (1 << LG) >> 4;
+    // last group: element m of thread t is coefficient t + m * N/16 (the factor
+    // 1/N was applied by the pointwise products)
+    const int64_t d0 = t - a.lo;
+    if (d0 >= 0 && d0 + 15 * TPT < a.cnt) {
+        // every slot of this thread is inside [lo, lo + cnt)
+        if (a.direct) {
+            uint64_t *o = a.out64 + e * a.out_ld + d0;
+#pragma unroll
+            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
+        } else {
+            uint32_t *o = a.res32 + (j * a.nent + e) * a.cnt + d0;
+#pragma unroll
+            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < 16; m++) {
+            const int64_t d = d0 + m * TPT;
+            if (d < 0 || d >= a.cnt) continue;
+            const uint32_t val = csub(csub(v[m], 2 * q), q);
+            if (a.direct)
+                a.out64[e * a.out_ld + d] = val;
+            else
+                a.res32[(j * a.nent + e) * a.cnt + d] = val;
+        }
+    }
+    if (a.direct)
+        for (int64_t d = a.cnt + t; d < a.out_cap; d += TPT) a.out64[e * a.out_ld + d] = 0;
+}
+
 template <int LG>
 __global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INV_MIN)
 ntt_inv_kernel(NttInvArgs a)
@@ -334,36 +375,56 @@ ntt_inv_kernel(NttInvArgs a)
         for (int m = 0; m < 16; m++) v[m] = 0;
     }
     inv_groups<LG, 0>(v, x, t, T);
-    // last group: element m of thread t is coefficient t + m * N/16 (the factor
-    // 1/N was applied by the pointwise products)
-    if (!active) return;
-    const uint32_t q = T.q;
-    const int64_t d0 = t - a.lo;
-    if (d0 >= 0 && d0 + 15 * TPT < a.cnt) {
-        // every slot of this thread is inside [lo, lo + cnt)
-        if (a.direct) {
-            uint64_t *o = a.out64 + e * a.out_ld + d0;
+    if (active) inv_store<LG>(v, a, e, j, t, T.q);
+}
+
+// Persistent inverse transforms, one transform per CTA at a time (N >= 4096):
+// while a transform is computed, the point tiles of the CTA's next one are
+// already on their way into shared memory (cp.async, 16-byte chunks; each
+// thread prefetches and later reads only its own four chunks, so the buffer
+// needs no barrier).
+template <int LG>
+__global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INVP_MIN)
+ntt_inv_persist_kernel(NttInvArgs a)
+{
+    extern __shared__ __align__(16) uint32_t smem[];
+    constexpr int N = 1 << LG, TPT = N >> 4;
+    static_assert(TPT >= 256, "one transform per CTA");
+    uint32_t *x = smem;
+    uint32_t *pf = smem + N + (N >> 4);
+    const int t = threadIdx.x, j = blockIdx.y;
+    const NttDev &T = a.tab[j];
+    const uint32_t *base = a.in + j * a.prime_stride;
+    // chunk c of thread t sits at 16 t + 4 (c ^ ((t >> 1) & 3)): conflict-free 16-byte reads
+    const int sw = (t >> 1) & 3;
+    const uint32_t pf_s = (uint32_t)__cvta_generic_to_shared(pf + 16 * t);
+    auto prefetch = [&](int64_t ee) {
+        const uint32_t *src = base + ee * kPtTile;
 #pragma unroll
-            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
-        } else {
-            uint32_t *o = a.res32 + (j * a.nent + e) * a.cnt + d0;
-#pragma unroll
-            for (int m = 0; m < 16; m++) o[m * TPT] = csub(csub(v[m], 2 * q), q);
+        for (int c = 0; c < 4; c++) {
+            const int pt = 16 * t + 4 * c;
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;"
+                         ::"r"(pf_s + 16u * (uint32_t)(c ^ sw)),
+                           "l"(src + (int64_t)(pt / kPtTile) * a.tile_stride + pt % kPtTile)
+                         : "memory");
         }
-    } else {
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    int64_t e = blockIdx.x;
+    if (e < a.nent) prefetch(e);
+    for (; e < a.nent; e += gridDim.x) {
+        asm volatile("cp.async.wait_group 0;" ::: "memory");
+        uint32_t v[16];
 #pragma unroll
-        for (int m = 0; m < 16; m++) {
-            const int64_t d = d0 + m * TPT;
-            if (d < 0 || d >= a.cnt) continue;
-            const uint32_t val = csub(csub(v[m], 2 * q), q);
-            if (a.direct)
-                a.out64[e * a.out_ld + d] = val;
-            else
-                a.res32[(j * a.nent + e) * a.cnt + d] = val;
+        for (int c = 0; c < 4; c++) {
+            const uint4 o = *reinterpret_cast<const uint4 *>(pf + 16 * t + 4 * (c ^ sw));
+            v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
         }
+        if (e + gridDim.x < a.nent) prefetch(e + gridDim.x);
+        inv_groups<LG, 0>(v, x, t, T);
+        inv_store<LG>(v, a, e, j, t, T.q);
     }
-    if (a.direct)
-        for (int64_t d = a.cnt + t; d < a.out_cap; d += TPT) a.out64[e * a.out_ld + d] = 0;
+    asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -442,6 +503,11 @@ static cudaError_t set_attrs()
     const int sm = (int)(((1 << LG) + (1 << (LG - 4))) * sizeof(uint32_t) * ((1 << (LG - 4)) >= 256 ? 1 : 256 >> (LG - 4)));
     cudaError_t e = cudaFuncSetAttribute(ntt_fwd_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(ntt_inv_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+    if constexpr (LG >= 12) {
+        const int smp = (int)(((1 << LG) + (1 << (LG - 4)) + (1 << LG)) * sizeof(uint32_t));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(ntt_inv_persist_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+    }
     return e;
 }
 
@@ -501,7 +567,22 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st)
     ntt_geometry(a.lg, a.nent, &threads, &tpc, &smem, &blocks);
     if (blocks > 0x7fffffffll) return PMLG_EUNSUP;
     prof_begin(ctx, "ntt_inv", st);
-    NTT_DISPATCH(ntt_inv_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);
+    if (PMLG_NTT_INV_PERSIST && a.lg >= 12) {
+        // persistent: as many CTAs as fit on the GPU, each walking over transforms
+        const int N = 1 << a.lg;
+        const size_t smp = (size_t)(2 * N + (N >> 4)) * sizeof(uint32_t);
+        const int per_sm = a.lg == 12 ? 6 : a.lg == 13 ? 3 : 1;
+        int64_t g = (int64_t)ctx->sm_count * per_sm;
+        if (g > a.nent) g = a.nent;
+        const dim3 grid((unsigned)g, a.t);
+        switch (a.lg) {
+        case 12: ntt_inv_persist_kernel<12><<<grid, N >> 4, smp, st>>>(a); break;
+        case 13: ntt_inv_persist_kernel<13><<<grid, N >> 4, smp, st>>>(a); break;
+        default: ntt_inv_persist_kernel<14><<<grid, N >> 4, smp, st>>>(a); break;
+        }
+    } else {
+        NTT_DISPATCH(ntt_inv_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);
+    }
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
