@@ -16,6 +16,10 @@
 // (q < 2^30, lazy reduction).
 #include "ntt.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cstring>
+
 namespace pmlg {
 
 __device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
@@ -236,6 +240,9 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
 #ifndef PMLG_NTT_INV_REGS
 #define PMLG_NTT_INV_REGS 40
 #endif
+#ifndef PMLG_NTT_FWD_TMA
+#define PMLG_NTT_FWD_TMA 1       // forward evaluations leave through TMA tensor stores for N >= 4096
+#endif
 #ifndef PMLG_NTT_INV_PERSIST
 #define PMLG_NTT_INV_PERSIST 1   // persistent, prefetching inverse kernel for N >= 4096
 #endif
@@ -278,7 +285,7 @@ __device__ __forceinline__ void fwd_transform(uint32_t (&v)[16], uint32_t *x, in
 
 template <int LG>
 __global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::FWD_MIN)
-ntt_fwd_kernel(NttFwdArgs a)
+ntt_fwd_kernel(NttFwdArgs a, const __grid_constant__ CUtensorMap tmap)
 {
     extern __shared__ uint32_t smem[];
     constexpr int N = 1 << LG, TPT = N >> 4;
@@ -296,6 +303,36 @@ ntt_fwd_kernel(NttFwdArgs a)
     else
         fwd_transform<LG, false>(v, x, t, T, a, active, e);
     // the last group leaves points 16t .. 16t+15 in v[0..15]
+    if constexpr (LG >= 12) {
+        // One transform per CTA: the evaluations are staged in the exchange buffer
+        // (thread t: tiles 4t..4t+3, 64 contiguous bytes) and the tensor-memory
+        // accelerator scatters the 16-byte point tiles, 256 tiles per box.
+        const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(x);
+        if (a.use_tma && (sbase & 127u) == 0) {
+            const uint32_t q = T.q;
+            __syncthreads();   // every thread is done reading the last layout
+            uint4 *stg = reinterpret_cast<uint4 *>(x) + 4 * t;
+#pragma unroll
+            for (int c = 0; c < 4; c++)
+                stg[c] = make_uint4(csub(v[4 * c + 0], q), csub(v[4 * c + 1], q), csub(v[4 * c + 2], q),
+                                    csub(v[4 * c + 3], q));
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                constexpr int NT = N / kPtTile, NBOX = NT / 256;
+                const int z0 = j * NT;
+#pragma unroll 1
+                for (int b = 0; b < NBOX; b++)
+                    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];"
+                                 ::"l"(&tmap), "r"(0), "r"((int)e), "r"(z0 + 256 * b),
+                                   "r"(sbase + (uint32_t)b * 256u * kPtTile * 4u)
+                                 : "memory");
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+                asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");   // smem stays live until read
+            }
+            return;
+        }
+    }
     if (active) {
         uint32_t *dst = a.out + j * a.prime_stride + e * kPtTile;
         const uint32_t q = T.q;
@@ -523,33 +560,68 @@ static int ensure_smem_attr(pmlg_ctx *ctx)
     return PMLG_OK;
 }
 
-#define NTT_DISPATCH(KERNEL, LGV, GRID, TH, SMEM, ST, ARGS)                      \
+#define NTT_DISPATCH(KERNEL, LGV, GRID, TH, SMEM, ST, ...)                       \
     switch (LGV) {                                                                \
-    case 4: KERNEL<4><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 5: KERNEL<5><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 6: KERNEL<6><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 7: KERNEL<7><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 8: KERNEL<8><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 9: KERNEL<9><<<GRID, TH, SMEM, ST>>>(ARGS); break;                       \
-    case 10: KERNEL<10><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
-    case 11: KERNEL<11><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
-    case 12: KERNEL<12><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
-    case 13: KERNEL<13><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
-    default: KERNEL<14><<<GRID, TH, SMEM, ST>>>(ARGS); break;                     \
+    case 4: KERNEL<4><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 5: KERNEL<5><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 6: KERNEL<6><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 7: KERNEL<7><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 8: KERNEL<8><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 9: KERNEL<9><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;                \
+    case 10: KERNEL<10><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;              \
+    case 11: KERNEL<11><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;              \
+    case 12: KERNEL<12><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;              \
+    case 13: KERNEL<13><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;              \
+    default: KERNEL<14><<<GRID, TH, SMEM, ST>>>(__VA_ARGS__); break;              \
     }
 
-int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a, cudaStream_t st)
+// cuTensorMapEncodeTiled from the driver, looked up once
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
 {
-    if (a.lg < kMinLgN || a.lg > kMaxLgN) return PMLG_ELEN;
-    if (a.nent <= 0) return PMLG_OK;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult qr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &qr) ==
+                cudaSuccess &&
+            qr == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a0, cudaStream_t st)
+{
+    if (a0.lg < kMinLgN || a0.lg > kMaxLgN) return PMLG_ELEN;
+    if (a0.nent <= 0) return PMLG_OK;
     PMLG_TRY(ensure_smem_attr(ctx));
     int threads, tpc;
     size_t smem;
     int64_t blocks;
-    ntt_geometry(a.lg, a.nent, &threads, &tpc, &smem, &blocks);
+    ntt_geometry(a0.lg, a0.nent, &threads, &tpc, &smem, &blocks);
     if (blocks > 0x7fffffffll) return PMLG_EUNSUP;
+    NttFwdArgs a = a0;
+    // N >= 4096: a 3-D tensor map over the evaluations, (point in tile, entry, tile of any
+    // prime), box (kPtTile, 1, 256); without it the kernel stores the tiles itself
+    alignas(64) CUtensorMap tmap;
+    std::memset(&tmap, 0, sizeof(tmap));
+    a.use_tma = 0;
+    if (PMLG_NTT_FWD_TMA && a.lg >= 12 && a.nent <= 0x7fffffffll) {
+        PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+        const cuuint64_t ntiles = ((cuuint64_t)1 << a.lg) / kPtTile * (cuuint64_t)a.t;
+        const cuuint64_t gdim[3] = {(cuuint64_t)kPtTile, (cuuint64_t)a.nent, ntiles};
+        const cuuint64_t gstride[2] = {(cuuint64_t)kPtTile * 4u, (cuuint64_t)a.tile_stride * 4u};
+        const cuuint32_t box[3] = {(cuuint32_t)kPtTile, 1u, 256u}, estride[3] = {1u, 1u, 1u};
+        if (enc && ((uintptr_t)a.out & 15u) == 0 && a.prime_stride == ((int64_t)1 << a.lg) / kPtTile * a.tile_stride &&
+            enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, a.out, gdim, gstride, box, estride,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+            a.use_tma = 1;
+    }
     prof_begin(ctx, "ntt_fwd", st);
-    NTT_DISPATCH(ntt_fwd_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);
+    NTT_DISPATCH(ntt_fwd_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a, tmap);
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());

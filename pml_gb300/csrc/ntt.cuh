@@ -51,6 +51,7 @@ struct NttFwdArgs
     uint32_t *out;
     int64_t prime_stride, tile_stride;
     int lg, t, reduce;      // reduce: inputs are < 2^64 and need reduction mod q
+    int use_tma;            // N >= 4096: evaluations leave through TMA tensor stores (set by ntt_forward)
     NttDev tab[kMaxPrimes];
 };
 
