@@ -243,6 +243,9 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
 #ifndef PMLG_NTT_FWD_TMA
 #define PMLG_NTT_FWD_TMA 1       // forward evaluations leave through TMA tensor stores for N >= 4096
 #endif
+#ifndef PMLG_NTT_INV_TMA
+#define PMLG_NTT_INV_TMA 1       // persistent inverse: point tiles brought in by TMA tensor loads
+#endif
 #ifndef PMLG_NTT_INV_PERSIST
 #define PMLG_NTT_INV_PERSIST 1   // persistent, prefetching inverse kernel for N >= 4096
 #endif
@@ -464,6 +467,70 @@ ntt_inv_persist_kernel(NttInvArgs a)
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
+// The same, with the point tiles brought in by TMA tensor loads (256 tiles per
+// box, one transform = N / 1024 boxes) completing on an mbarrier; the wait is
+// bounded (on time-out the error word is set and the results are invalid).
+template <int LG>
+__global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INVP_MIN)
+ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
+{
+    extern __shared__ __align__(128) uint32_t smem[];
+    constexpr int N = 1 << LG, NT = N / kPtTile, NBOX = NT / 256;
+    constexpr uint32_t BYTES = (uint32_t)N * 4u;
+    uint32_t *x = smem;
+    uint32_t *pf = smem + N + (N >> 4);                 // N + N/16 words: a multiple of 128 bytes
+    __shared__ __align__(8) uint64_t bar;
+    const int t = threadIdx.x, j = blockIdx.y;
+    const NttDev &T = a.tab[j];
+    const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(&bar);
+    const uint32_t pf_s = (uint32_t)__cvta_generic_to_shared(pf);
+    if (pf_s & 127u) {   // a TMA destination must be 128-byte aligned: report and do nothing
+        if (t == 0 && a.err) atomicExch(a.err, 1);
+        return;
+    }
+    if (t == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s));
+        asm volatile("fence.mbarrier_init.release.cluster;");
+    }
+    __syncthreads();
+    auto prefetch = [&](int64_t ee) {   // one thread
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s), "r"(BYTES) : "memory");
+#pragma unroll 1
+        for (int b = 0; b < NBOX; b++)
+            asm volatile("cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+                         ::"r"(pf_s + (uint32_t)b * 256u * kPtTile * 4u), "l"(&tmap), "r"(0), "r"((int)ee),
+                           "r"(j * NT + 256 * b), "r"(bar_s)
+                         : "memory");
+    };
+    int64_t e = blockIdx.x;
+    if (e < a.nent && t == 0) prefetch(e);
+    uint32_t phase = 0;
+    for (; e < a.nent; e += gridDim.x, phase ^= 1u) {
+        uint32_t done = 0;
+        unsigned long long t0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        for (int it = 0; it < (1 << 24) && !done; it++) {
+            asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+                         : "=r"(done) : "r"(bar_s), "r"(phase) : "memory");
+            unsigned long long tn;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(tn));
+            if (tn - t0 > 500000000ull) break;
+        }
+        if (!done && a.err) atomicExch(a.err, 1);
+        uint32_t v[16];
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            const uint4 o = *reinterpret_cast<const uint4 *>(pf + 16 * t + 4 * c);
+            v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
+        }
+        __syncthreads();   // the buffer is read: the next transform may come in
+        if (t == 0 && done && e + gridDim.x < a.nent) prefetch(e + gridDim.x);
+        inv_groups<LG, 0>(v, x, t, T);
+        inv_store<LG>(v, a, e, j, t, T.q);
+        if (!__syncthreads_and(done)) break;   // a load that never completed ends the CTA's work
+    }
+}
+
 // ---------------------------------------------------------------------------
 
 __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int64_t nent, int64_t cnt,
@@ -544,6 +611,8 @@ static cudaError_t set_attrs()
         const int smp = (int)(((1 << LG) + (1 << (LG - 4)) + (1 << LG)) * sizeof(uint32_t));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(ntt_inv_persist_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(ntt_inv_tma_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
     }
     return e;
 }
@@ -628,8 +697,10 @@ int ntt_forward(pmlg_ctx *ctx, const NttFwdArgs &a0, cudaStream_t st)
     return PMLG_OK;
 }
 
-int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st)
+int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a0, cudaStream_t st)
 {
+    NttInvArgs a = a0;
+    a.err = ctx->d_err;
     if (a.lg < kMinLgN || a.lg > kMaxLgN) return PMLG_ELEN;
     if (a.nent <= 0) return PMLG_OK;
     PMLG_TRY(ensure_smem_attr(ctx));
@@ -647,10 +718,34 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a, cudaStream_t st)
         int64_t g = (int64_t)ctx->sm_count * per_sm;
         if (g > a.nent) g = a.nent;
         const dim3 grid((unsigned)g, a.t);
-        switch (a.lg) {
-        case 12: ntt_inv_persist_kernel<12><<<grid, N >> 4, smp, st>>>(a); break;
-        case 13: ntt_inv_persist_kernel<13><<<grid, N >> 4, smp, st>>>(a); break;
-        default: ntt_inv_persist_kernel<14><<<grid, N >> 4, smp, st>>>(a); break;
+        // the point tiles come in by TMA when a tensor map over them can be made:
+        // (point in tile, entry, tile of any prime), box (kPtTile, 1, 256)
+        alignas(64) CUtensorMap tmap;
+        std::memset(&tmap, 0, sizeof(tmap));
+        bool tma = false;
+        if (PMLG_NTT_INV_TMA && a.nent <= 0x7fffffffll) {
+            PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+            const cuuint64_t ntiles = (cuuint64_t)N / kPtTile * (cuuint64_t)a.t;
+            const cuuint64_t gdim[3] = {(cuuint64_t)kPtTile, (cuuint64_t)a.nent, ntiles};
+            const cuuint64_t gstride[2] = {(cuuint64_t)kPtTile * 4u, (cuuint64_t)a.tile_stride * 4u};
+            const cuuint32_t box[3] = {(cuuint32_t)kPtTile, 1u, 256u}, estride[3] = {1u, 1u, 1u};
+            tma = enc && ((uintptr_t)a.in & 15u) == 0 && a.prime_stride == (int64_t)N / kPtTile * a.tile_stride &&
+                  enc(&tmap, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, (void *)a.in, gdim, gstride, box, estride,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        }
+        if (tma) {
+            switch (a.lg) {
+            case 12: ntt_inv_tma_kernel<12><<<grid, N >> 4, smp, st>>>(a, tmap); break;
+            case 13: ntt_inv_tma_kernel<13><<<grid, N >> 4, smp, st>>>(a, tmap); break;
+            default: ntt_inv_tma_kernel<14><<<grid, N >> 4, smp, st>>>(a, tmap); break;
+            }
+        } else {
+            switch (a.lg) {
+            case 12: ntt_inv_persist_kernel<12><<<grid, N >> 4, smp, st>>>(a); break;
+            case 13: ntt_inv_persist_kernel<13><<<grid, N >> 4, smp, st>>>(a); break;
+            default: ntt_inv_persist_kernel<14><<<grid, N >> 4, smp, st>>>(a); break;
+            }
         }
     } else {
         NTT_DISPATCH(ntt_inv_kernel, a.lg, dim3((unsigned)blocks, a.t), threads, smem, st, a);

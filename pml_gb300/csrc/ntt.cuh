@@ -67,6 +67,7 @@ struct NttInvArgs
     // CRT output (otherwise): res32[(j * nent + e) * cnt + d]
     uint32_t *res32;
     int lg, t, direct;
+    int *err;               // device error word (a bounded wait gave up); set by ntt_inverse
     NttDev tab[kMaxPrimes];
 };
 
