@@ -284,8 +284,10 @@ pw_cc2_kernel(PwArgs a)
 //                soon as it is drained, and commits to the mbarriers.
 // Digits reach FP16 without conversion instructions: 0x6400 + u is the FP16
 // encoding of 1024 + u for 0 <= u <= 1024, and one packed subtraction removes
-// the bias.  The FP32 sums come back as integers the same way: for |S| <= 2^22
-// the encoding of S + 1.5 * 2^23 is 0x4B400000 + S.
+// the bias.  The FP32 sums come back as integers the same way: a first MMA
+// with constant operands puts 1.5 * 2^23 into every accumulator, and for
+// |S| <= 2^22 the encoding of 1.5 * 2^23 + S is 0x4B400000 + S (every partial
+// sum stays an integer in [2^23, 2^24], exact in FP32).
 // Every mbarrier wait is bounded; a wait that gives up raises a shared abort
 // flag that turns every later wait into a no-op, so all warps leave their
 // loops, the MMAs in flight are drained and the kernel records the error.
@@ -299,7 +301,8 @@ constexpr int F16_B_BYTES = 192 * 64 * 2;            // N = 2 regions x 96, K = 
 constexpr int F16_STAGE = 2 * F16_A_BYTES + F16_B_BYTES;
 constexpr int F16_CST_LD = 68;                       // padded staging row (words): conflict-free v4 stores
 constexpr int F16_CST_WORDS = 64 * F16_CST_LD;       // one (point, digit parity) plane
-constexpr int F16_SMEM = 2 * F16_STAGE + 4 * F16_CST_WORDS * 4 + 1024;   // + alignment slack
+constexpr int F16_BIAS_A = 128 * 16 * 2, F16_BIAS_B = 96 * 16 * 2;   // constant bias operands (K = 16)
+constexpr int F16_SMEM = 2 * F16_STAGE + 4 * F16_CST_WORDS * 4 + F16_BIAS_A + F16_BIAS_B + 1024;   // + alignment slack
 constexpr uint32_t F16_TMEM_COLS = 512;
 #ifndef PMLG_F16_SUSPEND_NS
 #define PMLG_F16_SUSPEND_NS 0
@@ -313,11 +316,11 @@ __device__ __forceinline__ uint32_t canon_off(int row, int k)
     return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
-__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr)
+__device__ __forceinline__ uint64_t umma_desc(uint32_t saddr, uint32_t sbo = 1024)
 {
-    // start address, LBO = 128 B (next core matrix along K), SBO = 1024 B (next 8 rows),
-    // descriptor version 1, no swizzle
-    return (uint64_t)((saddr >> 4) & 0x3fff) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+    // start address, LBO = 128 B (next core matrix along K), SBO (next 8 rows; 1024 B for
+    // K = 64 tiles), descriptor version 1, no swizzle
+    return (uint64_t)((saddr >> 4) & 0x3fff) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
            ((uint64_t)1 << 46);
 }
 
@@ -460,6 +463,16 @@ pw_f16_kernel(PwArgs a)
                      ::"r"((uint32_t)__cvta_generic_to_shared(&tmem_slot)), "r"(F16_TMEM_COLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
+    // Bias operands: every entry of A is 256 and of B 3072 (both exact in FP16), so one
+    // K = 16 MMA puts 16 x 256 x 3072 = 1.5 x 2^23 into every accumulator before the digit
+    // products; the sums then come back as integers straight from their FP32 bits
+    // (0x4B400000 + S for |S| <= 2^22).
+    {
+        uint32_t *bias = reinterpret_cast<uint32_t *>(sm + 2 * F16_STAGE + 4 * F16_CST_WORDS * 4);
+        for (int i = tid; i < (F16_BIAS_A + F16_BIAS_B) / 4; i += blockDim.x)
+            bias[i] = i < F16_BIAS_A / 4 ? 0x5C005C00u : 0x6A006A00u;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
     if (tid == 0) {
         for (int s = 0; s < 2; s++) {
             mbar_init(&full[s], F16_SPLIT_WARPS);
@@ -538,6 +551,8 @@ pw_f16_kernel(PwArgs a)
         // ---- MMA issue (one thread)
         if (lane == 0) {
             const uint32_t idesc = (1u << 4) | ((uint32_t)(96 >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);
+            const uint32_t bias_a = (uint32_t)__cvta_generic_to_shared(sm + 2 * F16_STAGE + 4 * F16_CST_WORDS * 4);
+            const uint64_t dba = umma_desc(bias_a, 256), dbb = umma_desc(bias_a + F16_BIAS_A, 256);
             uint32_t p = 0;
             int lc = 0;
             for (int64_t gc = blockIdx.x; gc < nunits; gc += gridDim.x, lc++) {
@@ -549,7 +564,12 @@ pw_f16_kernel(PwArgs a)
                         if (!ok) break;
                         asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
-                        for (int s = 0; s < 2; s++)
+                        for (int s = 0; s < 2; s++) {
+                            // the bias first (overwriting the accumulators), then the digit products
+                            asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+                                         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+                                         ::"r"(tmem + (uint32_t)(256 * h + 96 * s)), "l"(dba), "l"(dbb), "r"(idesc),
+                                           "r"(0u));
 #pragma unroll
                             for (int ks = 0; ks < 4; ks++) {
                                 const uint64_t da = umma_desc(base + s * F16_A_BYTES + ks * 256);
@@ -557,8 +577,9 @@ pw_f16_kernel(PwArgs a)
                                 asm volatile("{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
                                              "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
                                              ::"r"(tmem + (uint32_t)(256 * h + 96 * s)), "l"(da), "l"(db), "r"(idesc),
-                                               "r"((uint32_t)(ks > 0)));
+                                               "r"(1u));
                             }
+                        }
                         tc_commit(&tfull[h]);
                     }
                     if (ok) tc_commit(&empty[pp]);
@@ -604,8 +625,7 @@ pw_f16_kernel(PwArgs a)
                             for (int j = 0; j < 3; j++)
 #pragma unroll
                                 for (int u = 0; u < 16; u++)
-                                    acc[u] += (uint64_t)__float_as_uint(__fadd_rn(__uint_as_float(v[j][u]), 12582912.0f)) *
-                                              w[s][j];
+                                    acc[u] += (uint64_t)v[j][u] * w[s][j];   // bits = 0x4B400000 + S
                         }
                         asm volatile("tcgen05.fence::before_thread_sync;");
                     }
