@@ -241,8 +241,8 @@ def run_reference(args):
 # ncu capture of `python bench.py --profile-case product` (profiles/ntt_kernels_n8192_4096polys.md,
 # profiles/pointwise_kernels_64x64_8192pts.md); a cold, single capture, so part of the output is
 # still in L2 when the kernel ends
-NCU_TRAFFIC = {"ntt_fwd": 218.8e6, "ntt_inv": 346.5e6, "pointwise_f16_tc": 369.5e6,
-               "pointwise_int8_tc": 368.9e6, "pointwise_cuda_core": 366.7e6}
+NCU_TRAFFIC = {"ntt_fwd": 217.1e6, "ntt_inv": 360.3e6, "pointwise_f16_tc": 368.2e6,
+               "pointwise_int8_tc": 370.8e6, "pointwise_cuda_core": 367.1e6}
 
 
 def algorithmic_bytes(kernel: str):
