@@ -265,37 +265,46 @@ mbasis_leaf_kernel(LeafArgs a)
 }
 
 // ---------------------------------------------------------------------------
-// cluster leaf: m <= 64, n <= 32, order <= 32
+// cluster leaf: m <= 64, n <= 32, order <= 32, odd p
 // ---------------------------------------------------------------------------
 //
-// One leaf runs on a cluster of LC_CL CTAs (one per SM).  CTA c keeps, in its
-// own shared memory, the columns [c*ncm, (c+1)*ncm) of every coefficient of
-// appbas and the columns [c*ncn, (c+1)*ncn) of every coefficient of the
-// residual R.  Each step:
-//   1. every CTA computes the same stable shift permutation (rank counting,
-//      8 threads per row);
-//   2. every CTA writes its slice of the permuted R[ord] (transposed) into
-//      CTA 0's shared memory (distributed shared memory stores); cluster barrier;
-//   3. CTA 0 runs the elimination with its 16 warps: lane j holds row j of
-//      E = R[ord]^T (j < n <= 32), warp w holds columns [4w, 4w+4) in
-//      registers (LC_EW = 16 warps of 4 columns by default); column c's owner
-//      warp finds the pivot with a ballot and publishes it through shared
-//      memory (double-buffered, one barrier per column); every warp updates
-//      its columns with pivot row values taken by warp shuffles.  Updates are
-//      division-free,
-//      row_j <- (pv * row_j - f_j * row_pl) * 2^-32 mod p (Montgomery
-//      reduction): every row operation only scales rows, so the ratios
-//      E[pl_b][np_a] / E[pl_b][pc_b] at the end are the RREF entries.  Once
-//      every row holds a pivot, the remaining columns are non-pivots;
-//   4. CTA 0 computes X (pivot inverses by Montgomery exponentiation), the
-//      pivot rows and the exact appbas length; cluster barrier; every CTA
-//      copies them from CTA 0;
-//   5. every CTA updates its slices (non-pivot rows += X * pivot rows, a
-//      whole row slice per thread; pivot rows times x) and the shift, and
-//      reports to CTA 0 whether a pivot row reached appbas' top coefficient
-//      (the length grows by one when any did, nmod_mat_poly_mbasis.c:306-313).
+// One leaf runs on a cluster of 1 + LC_SL CTAs (one per SM), pipelined over the
+// order steps.  CTA 0, the eliminator, holds no slices.  Slice CTA 1+q keeps, in
+// its own shared memory, the columns [q*ncm, (q+1)*ncm) of every coefficient of
+// appbas and the columns [q*ncn, (q+1)*ncn) of every coefficient of the residual
+// R = appbas * F mod x^order, which every row operation keeps up to date (so the
+// residual of step s is R[s]).  Each step s has two cluster barrier phases:
+//   G_s  the slice CTAs have written the permuted R[s]^T into CTA 0's shared
+//        memory (distributed shared memory stores);
+//   X_s  CTA 0 has published the pivots and X of step s, and the slice CTAs have
+//        finished the update of step s-1.
+// CTA 0, between G_s and X_s: the elimination of R[s]^T, then X.  The slice CTAs,
+// after X_s: take the pivots and X; add one to the pivot rows' shifts; compute
+// the stable shift permutation of step s+1 and the one coefficient s+1 of the
+// updated residual (pivot rows take their coefficient s, non-pivot rows add X
+// times the pivot rows), write it into CTA 0 and arrive at G_{s+1}; then apply
+// the whole update of step s to their slices while CTA 0 eliminates step s+1.
+//
+// Elimination (CTA 0, its first LC_EW warps): lane j holds row j of E = R[s]^T
+// (j < n <= 32), warp w holds columns [4w, 4w+4) in registers (LC_EW = 16 warps
+// of 4 columns by default); column c's owner warp finds the pivot with a ballot
+// and publishes it through shared memory (double-buffered, one barrier per
+// column); every warp updates its columns with pivot row values taken by warp
+// shuffles.  Updates are division-free,
+//   row_j <- (pv * row_j - f_j * row_pl) * 2^-32 mod p   (Montgomery reduction):
+// every row operation only scales rows, so the ratios E[pl_b][np_a] / E[pl_b][pc_b]
+// at the end are the RREF entries.  Once every row holds a pivot, the remaining
+// columns are non-pivots.  X = -RREF restricted to the non-pivot columns, with
+// the pivot inverses by Montgomery exponentiation.
+//
+// Update of step s (slice CTAs): non-pivot rows += X * pivot rows (a whole row
+// slice per thread) on appbas' coefficients d < alen and R's coefficients past s;
+// pivot rows times x.  The length of appbas grows by one when a pivot row reaches
+// its top coefficient (nmod_mat_poly_mbasis.c:306-313): each slice CTA reports it
+// into CTA 0, and every slice CTA reads the flags after X_{s+1}.
 
-constexpr int LC_CL = 8;
+constexpr int LC_SL = 8;                 // slice CTAs
+constexpr int LC_CL = 1 + LC_SL;         // cluster size (a non-portable size, above 8)
 constexpr int LC_THREADS = 512;
 constexpr int LC_MAXM = 64, LC_MAXN = 32, LC_MAXORD = 32;
 #ifndef PMLG_LC_ELIM_WARPS
@@ -304,6 +313,7 @@ constexpr int LC_MAXM = 64, LC_MAXN = 32, LC_MAXORD = 32;
 // warps of CTA 0 that run the elimination (each holds 64 / LC_EW columns of E)
 constexpr int LC_EW = PMLG_LC_ELIM_WARPS, LC_CPW = LC_MAXM / LC_EW;
 static_assert(LC_EW == 4 || LC_EW == 8 || LC_EW == 16, "elimination warps");
+static_assert(LC_THREADS == 8 * LC_MAXM, "the permutation takes 8 threads per row");
 
 __device__ __forceinline__ uint32_t redc(uint64_t t, uint32_t p, uint32_t pneg)
 {
@@ -327,13 +337,24 @@ __device__ __forceinline__ uint32_t mont_pow(uint32_t b, uint32_t e, uint32_t p,
     return redc(rm, p, pneg);
 }
 
+// split cluster barrier: every thread of every CTA arrives, then waits for the phase
+__device__ __forceinline__ void cluster_arrive()
+{
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait()
+{
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 struct LcShared
 {
-    uint32_t E[LC_MAXN][LC_MAXM + 1];   // gathered R[ord]^T (CTA 0)
-    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank
+    uint32_t E[LC_MAXN][LC_MAXM + 1];   // CTA 0: gathered R[s]^T
+    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank (CTA 0 computes it, the slice CTAs copy it)
     int pivrow[LC_MAXM], nprow[LC_MAXM];
-    int info[3];                        // rank, nullity, appbas length for this step's update
-    int growf[LC_CL];                   // CTA 0: per-CTA "pivot row at the top coefficient" flags
+    int rowidx[LC_MAXM];                // slice CTAs: row -> its non-pivot index, -1 for a pivot row
+    int info[2];                        // CTA 0: rank and nullity of the current step
+    int growf[2][LC_SL];                // CTA 0: per-slice growth flags, by step parity
     long long sh[LC_MAXM];
     int perm[LC_MAXM];
     uint32_t fbuf[2][32];               // the current column's values, pivot value and
@@ -343,7 +364,212 @@ struct LcShared
     uint32_t inv[LC_MAXM];
 };
 
-__global__ void __cluster_dims__(LC_CL, 1, 1) __launch_bounds__(LC_THREADS)
+// stable shift permutation (rank counting, 8 threads per row): perm[r] = the row of rank r
+// (_find_shift_permutation, nmod_mat_poly_mbasis.c:69-114)
+__device__ __forceinline__ void lc_perm(LcShared &S, int m, int tid)
+{
+    const int i = tid >> 3, part = tid & 7;
+    int r = 0;
+    if (i < m) {
+        const long long v = S.sh[i];
+        for (int jj = part; jj < m; jj += 8) r += (S.sh[jj] < v) || (S.sh[jj] == v && jj < i);
+    }
+    r += __shfl_xor_sync(0xffffffffu, r, 1);
+    r += __shfl_xor_sync(0xffffffffu, r, 2);
+    r += __shfl_xor_sync(0xffffffffu, r, 4);
+    if (i < m && part == 0) S.perm[r] = i;
+}
+
+// CTA 0, step s: elimination of E = R[s]^T, pivots, X, and the shifts of the next
+// step.  S.perm holds the permutation of step s.  Ends with a block barrier.
+__device__ void lc_eliminate(LcShared &S, const LeafArgs &a, int s, int tid, int nth)
+{
+    const int m = a.m, n = a.n;
+    const uint32_t p = a.p;
+    const int w = tid >> 5, lane = tid & 31;
+    int rank = 0, nn = 0;
+    if (w < LC_EW) {
+        uint32_t x[LC_CPW];
+#pragma unroll
+        for (int k = 0; k < LC_CPW; k++)
+            x[k] = (lane < n && LC_CPW * w + k < m) ? S.E[lane][LC_CPW * w + k] : 0u;
+        unsigned used = 0;
+        for (int col = 0; col < m; col++) {
+            if (rank == n) {
+                // every row holds a pivot: the remaining columns are non-pivots
+                if (tid == 0) S.nonpiv[nn] = col;
+                nn++;
+                continue;
+            }
+            const int buf = col & 1, cw = col / LC_CPW, cl = col % LC_CPW;
+            if (w == cw) {
+                uint32_t v = x[0];
+#pragma unroll
+                for (int k = 1; k < LC_CPW; k++)
+                    if (cl == k) v = x[k];
+                const unsigned cand = __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
+                const int pl = cand ? __ffs(cand) - 1 : -1;
+                S.fbuf[buf][lane] = v;
+                if (lane == 0) S.plbuf[buf] = pl;
+                if (lane == pl) S.pvbuf[buf] = v;
+            }
+            if (LC_EW == 16)
+                __syncthreads();
+            else
+                asm volatile("bar.sync 1, %0;" ::"n"(LC_EW * 32) : "memory");
+            const int pl = S.plbuf[buf];
+            if (pl < 0) {
+                if (tid == 0) S.nonpiv[nn] = col;
+                nn++;
+                continue;
+            }
+            const uint32_t pv = S.pvbuf[buf];
+            const uint32_t f = S.fbuf[buf][lane];
+            const uint32_t nf = f ? p - f : 0u;
+#pragma unroll
+            for (int k = 0; k < LC_CPW; k++) {
+                const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
+                if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
+            }
+            used |= 1u << pl;
+            if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
+            rank++;
+        }
+#pragma unroll
+        for (int k = 0; k < LC_CPW; k++)
+            if (lane < n && LC_CPW * w + k < m) S.E[lane][LC_CPW * w + k] = x[k];
+    }
+    if (tid == 0) S.info[0] = rank;
+    __syncthreads();
+    rank = S.info[0];
+    const int nullity = m - rank;
+    if (tid < rank) S.pivrow[tid] = S.perm[S.pivcol[tid]];
+    if (tid < nullity) S.nprow[tid] = S.perm[S.nonpiv[tid]];
+    if (rank > 0 && nullity > 0) {
+        if (tid < rank) S.inv[tid] = mont_pow(S.E[S.pivlane[tid]][S.pivcol[tid]], p - 2, p, a.pneg, a.r2, a.r32);
+        __syncthreads();
+        for (int idx = tid; idx < nullity * rank; idx += nth) {
+            const int ia = idx / rank, b = idx - ia * rank;
+            const uint32_t v = mod64_q((uint64_t)S.E[S.pivlane[b]][S.nonpiv[ia]] * S.inv[b], p,
+                                       a.r32, a.r32q, a.oneq);
+            S.X[ia][b] = v ? p - v : 0u;
+        }
+    }
+    __syncthreads();
+    // shifts of the next step: pivot rows + 1; with no nullity, every row + (order - s)
+    if (tid == 0) S.info[1] = nullity;
+    if (nullity == 0) {
+        if (tid < m) S.sh[tid] += a.order - s;
+    } else if (tid < rank) {
+        S.sh[S.pivrow[tid]] += 1;
+    }
+    __syncthreads();
+}
+
+// slice CTA: the update of step s on its slices (non-pivot rows += X * pivot rows on
+// appbas' coefficients d < alen and R's coefficients s < d < order; pivot rows times
+// x).  Returns 1 when a pivot row was nonzero at coefficient alen-1 (appbas grows).
+__device__ int lc_update(LcShared &S, const LeafArgs &a, uint32_t *AB, uint32_t *R, int sab, int sr, int ncm, int ncn,
+                         int cm, int cn, bool vec, int rank, int nullity, int alen, int s, int tid, int nth)
+{
+    const uint32_t p = a.p;
+    const int order = a.order;
+    const int nab = nullity * alen;
+    const int nr = nullity * (order - s - 1);
+    for (int idx = tid; idx < nab + nr; idx += nth) {
+        const bool isab = idx < nab;
+        const int j2 = isab ? idx : idx - nab;
+        const int per = isab ? alen : (order - s - 1);
+        const int ia = j2 / per;
+        const int d = isab ? j2 - ia * per : s + 1 + (j2 - ia * per);
+        const int width = isab ? ncm : ncn, cols = isab ? cm : cn;
+        uint32_t *base = isab ? AB + (size_t)d * sab : R + (size_t)d * sr;
+        uint32_t *dst = base + S.nprow[ia] * width;
+        uint64_t acc[8];
+        if (vec) {
+            // whole rows of 4 or 8 words (columns past `cols` are zero padding)
+            const int nq = width >> 2;
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (h < nq) {
+                    const uint4 v = *reinterpret_cast<const uint4 *>(dst + 4 * h);
+                    acc[4 * h] = v.x; acc[4 * h + 1] = v.y; acc[4 * h + 2] = v.z; acc[4 * h + 3] = v.w;
+                } else {
+                    acc[4 * h] = acc[4 * h + 1] = acc[4 * h + 2] = acc[4 * h + 3] = 0;
+                }
+            for (int b0 = 0; b0 < rank; b0 += 8) {
+                const int bend = b0 + 8 < rank ? b0 + 8 : rank;
+                for (int b = b0; b < bend; b++) {
+                    const uint64_t xv = S.X[ia][b];
+                    const uint32_t *src = base + S.pivrow[b] * width;
+#pragma unroll
+                    for (int h = 0; h < 2; h++)
+                        if (h < nq) {
+                            const uint4 v = *reinterpret_cast<const uint4 *>(src + 4 * h);
+                            acc[4 * h] += xv * v.x; acc[4 * h + 1] += xv * v.y;
+                            acc[4 * h + 2] += xv * v.z; acc[4 * h + 3] += xv * v.w;
+                        }
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
+            }
+#pragma unroll
+            for (int h = 0; h < 2; h++)
+                if (h < nq) {
+                    uint4 v;
+                    v.x = mod64_q(acc[4 * h], p, a.r32, a.r32q, a.oneq);
+                    v.y = mod64_q(acc[4 * h + 1], p, a.r32, a.r32q, a.oneq);
+                    v.z = mod64_q(acc[4 * h + 2], p, a.r32, a.r32q, a.oneq);
+                    v.w = mod64_q(acc[4 * h + 3], p, a.r32, a.r32q, a.oneq);
+                    *reinterpret_cast<uint4 *>(dst + 4 * h) = v;
+                }
+            continue;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) acc[u] = (u < cols) ? dst[u] : 0ull;
+        for (int b0 = 0; b0 < rank; b0 += 8) {
+            const int bend = b0 + 8 < rank ? b0 + 8 : rank;
+            for (int b = b0; b < bend; b++) {
+                const uint64_t xv = S.X[ia][b];
+                const uint32_t *src = base + S.pivrow[b] * width;
+#pragma unroll
+                for (int u = 0; u < 8; u++)
+                    if (u < cols) acc[u] += xv * src[u];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++)
+            if (u < cols) dst[u] = mod64_q(acc[u], p, a.r32, a.r32q, a.oneq);
+    }
+    // growth test on this CTA's columns: a pivot row nonzero at coefficient alen-1
+    int grow = 0;
+    for (int idx = tid; idx < rank * cm; idx += nth) {
+        const int b = idx / cm, col = idx - b * cm;
+        if (AB[(size_t)(alen - 1) * sab + S.pivrow[b] * ncm + col] != 0) grow = 1;
+    }
+    grow = __syncthreads_or(grow);
+    // pivot rows times x (one coefficient more than the length: it may grow)
+    const int nlen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
+    for (int idx = tid; idx < rank * (cm + cn); idx += nth) {
+        const int b = idx / (cm + cn), col = idx - b * (cm + cn);
+        const int row = S.pivrow[b];
+        if (col < cm) {
+            for (int d = nlen - 1; d > 0; d--)
+                AB[(size_t)d * sab + row * ncm + col] = AB[(size_t)(d - 1) * sab + row * ncm + col];
+            AB[row * ncm + col] = 0;
+        } else {
+            const int j = col - cm;
+            for (int d = order - 1; d > s; d--)
+                R[(size_t)d * sr + row * ncn + j] = R[(size_t)(d - 1) * sr + row * ncn + j];
+        }
+    }
+    __syncthreads();
+    return grow;
+}
+
+__global__ void __launch_bounds__(LC_THREADS)
 mbasis_leaf_cluster_kernel(LeafArgs a)
 {
     namespace cg = cooperative_groups;
@@ -354,10 +580,11 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     const int tid = threadIdx.x, nth = blockDim.x;
     const int m = a.m, n = a.n, order = a.order;
     const uint32_t p = a.p;
-    const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
-    const int m0 = c * ncm, n0 = c * ncn;
-    const int cm = m0 < m ? (m - m0 < ncm ? m - m0 : ncm) : 0;
-    const int cn = n0 < n ? (n - n0 < ncn ? n - n0 : ncn) : 0;
+    const int ncm = (m + LC_SL - 1) / LC_SL, ncn = (n + LC_SL - 1) / LC_SL;
+    const int q = c - 1;                                     // slice index of a slice CTA
+    const int m0 = q * ncm, n0 = q * ncn;
+    const int cm = (c > 0 && m0 < m) ? (m - m0 < ncm ? m - m0 : ncm) : 0;
+    const int cn = (c > 0 && n0 < n) ? (n - n0 < ncn ? n - n0 : ncn) : 0;
     // coefficient d of the slices starts at d * sab (appbas) and d * sr (R).  The
     // padding makes threads working on consecutive coefficients of the same row
     // hit distinct banks: 4 words when the slice rows are whole 16-byte vectors
@@ -368,272 +595,128 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
     uint32_t *R = dyn + (size_t)(order + 1) * sab;           // [order][m][ncn], padded
     const int64_t fl = a.flen < order ? a.flen : order;
 
-    for (int idx = tid; idx < order * m * ncn; idx += nth) {
-        const int d = idx / (m * ncn), rem = idx - d * m * ncn, i = rem / ncn, jl = rem - i * ncn;
-        uint32_t v = 0;
-        if (jl < cn && d < fl) v = (uint32_t)a.F[((int64_t)i * n + n0 + jl) * a.ldF + d];
-        R[(size_t)d * sr + rem] = v;
-    }
-    for (int idx = tid; idx < (order + 1) * m * ncm; idx += nth) {
-        const int d = idx / (m * ncm), rem = idx - d * m * ncm, i = rem / ncm, il = rem - i * ncm;
-        AB[(size_t)d * sab + rem] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
+    if (c > 0) {
+        for (int idx = tid; idx < order * m * ncn; idx += nth) {
+            const int d = idx / (m * ncn), rem = idx - d * m * ncn, i = rem / ncn, jl = rem - i * ncn;
+            uint32_t v = 0;
+            if (jl < cn && d < fl) v = (uint32_t)a.F[((int64_t)i * n + n0 + jl) * a.ldF + d];
+            R[(size_t)d * sr + rem] = v;
+        }
+        for (int idx = tid; idx < (order + 1) * m * ncm; idx += nth) {
+            const int d = idx / (m * ncm), rem = idx - d * m * ncm, i = rem / ncm, il = rem - i * ncm;
+            AB[(size_t)d * sab + rem] = (d == 0 && il < cm && i == m0 + il) ? 1u : 0u;
+        }
     }
     if (tid < m) S.sh[tid] = a.shift[tid];
-    if (tid < LC_CL) S.growf[tid] = 0;
-    if (tid == 0) S.info[2] = 1;
-    int alen = 1;              // exact length of appbas, identical in every CTA
     uint32_t *E0 = cluster.map_shared_rank(&S.E[0][0], 0);
-    int *growf0 = cluster.map_shared_rank(S.growf, 0);
-    cluster.sync();
+    int *growf0 = cluster.map_shared_rank(&S.growf[0][0], 0);
+    int alen = 1;              // exact length of appbas (slice CTAs)
+    cluster.sync();            // every CTA runs before distributed shared memory is addressed
 
-    for (int ord = 0; ord < order; ord++) {
-        // 1. stable shift permutation (identical in every CTA): 8 threads per row
-        if (tid < 8 * LC_MAXM) {
-            const int i = tid >> 3, part = tid & 7;
-            int r = 0;
-            if (i < m) {
-                const long long v = S.sh[i];
-                for (int jj = part; jj < m; jj += 8) r += (S.sh[jj] < v) || (S.sh[jj] == v && jj < i);
-            }
-            r += __shfl_xor_sync(0xffffffffu, r, 1);
-            r += __shfl_xor_sync(0xffffffffu, r, 2);
-            r += __shfl_xor_sync(0xffffffffu, r, 4);
-            if (i < m && part == 0) S.perm[r] = i;
-        }
+    if (c > 0) {
+        // R[0]^T, permuted, into CTA 0
+        lc_perm(S, m, tid);
         __syncthreads();
-        // 2. gather the permuted R[ord]^T into CTA 0
         for (int idx = tid; idx < m * cn; idx += nth) {
             const int r = idx / cn, jl = idx - r * cn;
-            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[(size_t)ord * sr + S.perm[r] * ncn + jl];
+            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[S.perm[r] * ncn + jl];
         }
-        cluster.sync();
-
-        // 3. elimination in CTA 0 (its first LC_EW warps)
+    }
+    bool pending = false;      // slice CTAs: the update of the previous step is still to apply
+    int prank = 0, pnull = 0;  // its rank and nullity
+    for (int s = 0; s < order; s++) {
         if (c == 0) {
-            const int w = tid >> 5, lane = tid & 31;
-            int rank = 0, nn = 0;
-            if (w < LC_EW) {
-                uint32_t x[LC_CPW];
-#pragma unroll
-                for (int k = 0; k < LC_CPW; k++)
-                    x[k] = (lane < n && LC_CPW * w + k < m) ? S.E[lane][LC_CPW * w + k] : 0u;
-                unsigned used = 0;
-                for (int col = 0; col < m; col++) {
-                    if (rank == n) {
-                        // every row holds a pivot: the remaining columns are non-pivots
-                        if (tid == 0) S.nonpiv[nn] = col;
-                        nn++;
-                        continue;
-                    }
-                    const int buf = col & 1, cw = col / LC_CPW, cl = col % LC_CPW;
-                    if (w == cw) {
-                        uint32_t v = x[0];
-#pragma unroll
-                        for (int k = 1; k < LC_CPW; k++)
-                            if (cl == k) v = x[k];
-                        const unsigned cand = __ballot_sync(0xffffffffu, v != 0 && lane < n && !((used >> lane) & 1u));
-                        const int pl = cand ? __ffs(cand) - 1 : -1;
-                        S.fbuf[buf][lane] = v;
-                        if (lane == 0) S.plbuf[buf] = pl;
-                        if (lane == pl) S.pvbuf[buf] = v;
-                    }
-                    if (LC_EW == 16)
-                        __syncthreads();
-                    else
-                        asm volatile("bar.sync 1, %0;" ::"n"(LC_EW * 32) : "memory");
-                    const int pl = S.plbuf[buf];
-                    if (pl < 0) {
-                        if (tid == 0) S.nonpiv[nn] = col;
-                        nn++;
-                        continue;
-                    }
-                    const uint32_t pv = S.pvbuf[buf];
-                    const uint32_t f = S.fbuf[buf][lane];
-                    const uint32_t nf = f ? p - f : 0u;
-#pragma unroll
-                    for (int k = 0; k < LC_CPW; k++) {
-                        const uint32_t xp = __shfl_sync(0xffffffffu, x[k], pl);
-                        if (lane != pl) x[k] = redc((uint64_t)x[k] * pv + (uint64_t)nf * xp, p, a.pneg);
-                    }
-                    used |= 1u << pl;
-                    if (tid == 0) { S.pivlane[rank] = pl; S.pivcol[rank] = col; }
-                    rank++;
-                }
-#pragma unroll
-                for (int k = 0; k < LC_CPW; k++)
-                    if (lane < n && LC_CPW * w + k < m) S.E[lane][LC_CPW * w + k] = x[k];
-            }
-            if (tid == 0) S.info[0] = rank;
-            __syncthreads();
-            rank = S.info[0];
-            const int nullity = m - rank;
-            if (rank > 0 && nullity > 0) {
-                if (tid < rank) {
-                    S.inv[tid] = mont_pow(S.E[S.pivlane[tid]][S.pivcol[tid]], p - 2, p, a.pneg, a.r2, a.r32);
-                    S.pivrow[tid] = S.perm[S.pivcol[tid]];
-                }
-                if (tid < nullity) S.nprow[tid] = S.perm[S.nonpiv[tid]];
-                __syncthreads();
-                for (int idx = tid; idx < nullity * rank; idx += nth) {
-                    const int ia = idx / rank, b = idx - ia * rank;
-                    const uint32_t v = mod64_q((uint64_t)S.E[S.pivlane[b]][S.nonpiv[ia]] * S.inv[b], p,
-                                               a.r32, a.r32q, a.oneq);
-                    S.X[ia][b] = v ? p - v : 0u;
-                }
-            }
-            if (tid == 0) {
-                S.info[0] = rank;
-                S.info[1] = nullity;
-                // length of appbas after the previous step: it grew if a pivot row
-                // reached the top coefficient in any CTA
-                int g = 0;
-                for (int cc = 0; cc < LC_CL; cc++) g |= S.growf[cc];
-                S.info[2] += g;
-            }
+            lc_perm(S, m, tid);
+            cluster_arrive();
+            cluster_wait();                              // G_s
+            lc_eliminate(S, a, s, tid, nth);
+            cluster_arrive();
+            cluster_wait();                              // X_s
+            if (S.info[1] == 0) break;
+            continue;
         }
-        cluster.sync();
-
-        // 4. every CTA takes rank, pivots, X and the length from CTA 0
-        if (c != 0) {
-            const int *info0 = cluster.map_shared_rank(S.info, 0);
-            const int rk = info0[0], nl = info0[1];
-            if (tid < 3) S.info[tid] = info0[tid];
-            if (rk > 0 && nl > 0) {
-                const int *pr0 = cluster.map_shared_rank(S.pivrow, 0);
-                const int *np0 = cluster.map_shared_rank(S.nprow, 0);
-                const uint32_t *X0 = cluster.map_shared_rank(&S.X[0][0], 0);
-                if (tid < rk) S.pivrow[tid] = pr0[tid];
-                if (tid < nl) S.nprow[tid] = np0[tid];
-                for (int idx = tid; idx < nl * rk; idx += nth) {
-                    const int ia = idx / rk, b = idx - ia * rk;
-                    S.X[ia][b] = X0[ia * LC_MAXM + b];
-                }
-            }
-        }
-        __syncthreads();
-        const int rank = S.info[0], nullity = S.info[1];
-        alen = S.info[2];
+        cluster_arrive();                                // G_s: this CTA's part of R[s]^T is in CTA 0
+        int grow = 0;
+        if (pending) grow = lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, s - 1, tid, nth);
+        if (pending && tid == 0) growf0[((s - 1) & 1) * LC_SL + q] = grow;
+        cluster_wait();
+        cluster_arrive();
+        cluster_wait();                                  // X_s
+        // the growth of step s-1 in any slice, then rank, pivots and X of step s
+        if (pending)
+            alen += __syncthreads_or(tid < LC_SL ? growf0[((s - 1) & 1) * LC_SL + tid] : 0);
+        const int *info0 = cluster.map_shared_rank(S.info, 0);
+        const int rank = info0[0], nullity = info0[1];
         if (nullity == 0) {
-            // appbas = x^(order-ord) * appbas, shift += order - ord
-            const int k = order - ord;
+            // appbas = x^(order-s) * appbas, shift += order - s (nmod_mat_poly_mbasis.c:221-259)
+            const int k = order - s;
             for (int idx = tid; idx < m * ncm; idx += nth) {
                 for (int d = alen - 1; d >= 0; d--) AB[((size_t)(d + k)) * sab + idx] = AB[(size_t)d * sab + idx];
                 for (int d = 0; d < k; d++) AB[(size_t)d * sab + idx] = 0;
             }
             if (tid < m) S.sh[tid] += k;
             alen += k;
+            pending = false;
             __syncthreads();
             break;
         }
-        if (rank == 0) {
-            if (tid == 0) growf0[c] = 0;
-            continue;
+        if (rank > 0) {
+            const int *pr0 = cluster.map_shared_rank(S.pivrow, 0);
+            const int *np0 = cluster.map_shared_rank(S.nprow, 0);
+            const uint32_t *X0 = cluster.map_shared_rank(&S.X[0][0], 0);
+            if (tid < rank) S.pivrow[tid] = pr0[tid];
+            if (tid < nullity) S.nprow[tid] = np0[tid];
+            for (int idx = tid; idx < nullity * rank; idx += nth) {
+                const int ia = idx / rank, b = idx - ia * rank;
+                S.X[ia][b] = X0[ia * LC_MAXM + b];
+            }
+            __syncthreads();
+            if (tid < m) S.rowidx[tid] = -1;
+            if (tid < rank) S.sh[S.pivrow[tid]] += 1;
+            __syncthreads();
+            if (tid < nullity) S.rowidx[S.nprow[tid]] = tid;
         }
-
-        // 5a. non-pivot rows += X * pivot rows: one (row, coefficient) slice per item,
-        //     appbas coefficients d < alen, R coefficients ord < d < order
-        const int nab = nullity * alen;
-        const int nr = nullity * (order - ord - 1);
-        int grow = 0;
-        for (int idx = tid; idx < nab + nr; idx += nth) {
-            const bool isab = idx < nab;
-            const int j2 = isab ? idx : idx - nab;
-            const int per = isab ? alen : (order - ord - 1);
-            const int ia = j2 / per;
-            const int d = isab ? j2 - ia * per : ord + 1 + (j2 - ia * per);
-            const int width = isab ? ncm : ncn, cols = isab ? cm : cn;
-            uint32_t *base = isab ? AB + (size_t)d * sab : R + (size_t)d * sr;
-            uint32_t *dst = base + S.nprow[ia] * width;
-            uint64_t acc[8];
-            if (vec) {
-                // whole rows of 4 or 8 words (columns past `cols` are zero padding)
-                const int nq = width >> 2;
-#pragma unroll
-                for (int h = 0; h < 2; h++)
-                    if (h < nq) {
-                        const uint4 v = *reinterpret_cast<const uint4 *>(dst + 4 * h);
-                        acc[4 * h] = v.x; acc[4 * h + 1] = v.y; acc[4 * h + 2] = v.z; acc[4 * h + 3] = v.w;
-                    } else {
-                        acc[4 * h] = acc[4 * h + 1] = acc[4 * h + 2] = acc[4 * h + 3] = 0;
+        pending = rank > 0;
+        prank = rank;
+        pnull = nullity;
+        if (s + 1 < order) {
+            // coefficient s+1 of the residual after step s, permuted and transposed, into CTA 0
+            lc_perm(S, m, tid);
+            __syncthreads();
+            for (int idx = tid; idx < m * cn; idx += nth) {
+                const int r = idx / cn, jl = idx - r * cn;
+                const int i = S.perm[r];
+                const uint32_t *Rn = R + (size_t)(s + 1) * sr;
+                uint32_t v;
+                const int ia = rank > 0 ? S.rowidx[i] : 0;
+                if (rank == 0) {
+                    v = Rn[i * ncn + jl];
+                } else if (ia < 0) {
+                    v = R[(size_t)s * sr + i * ncn + jl];          // pivot row times x
+                } else {
+                    uint64_t acc = Rn[i * ncn + jl];
+                    for (int b0 = 0; b0 < rank; b0 += 8) {
+                        const int bend = b0 + 8 < rank ? b0 + 8 : rank;
+                        for (int b = b0; b < bend; b++) acc += (uint64_t)S.X[ia][b] * Rn[S.pivrow[b] * ncn + jl];
+                        acc = fold(acc, a.r32);
                     }
-                for (int b0 = 0; b0 < rank; b0 += 8) {
-                    const int bend = b0 + 8 < rank ? b0 + 8 : rank;
-                    for (int b = b0; b < bend; b++) {
-                        const uint64_t xv = S.X[ia][b];
-                        const uint32_t *src = base + S.pivrow[b] * width;
-#pragma unroll
-                        for (int h = 0; h < 2; h++)
-                            if (h < nq) {
-                                const uint4 v = *reinterpret_cast<const uint4 *>(src + 4 * h);
-                                acc[4 * h] += xv * v.x; acc[4 * h + 1] += xv * v.y;
-                                acc[4 * h + 2] += xv * v.z; acc[4 * h + 3] += xv * v.w;
-                            }
-                    }
-#pragma unroll
-                    for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
+                    v = mod64_q(acc, p, a.r32, a.r32q, a.oneq);
                 }
-#pragma unroll
-                for (int h = 0; h < 2; h++)
-                    if (h < nq) {
-                        uint4 v;
-                        v.x = mod64_q(acc[4 * h], p, a.r32, a.r32q, a.oneq);
-                        v.y = mod64_q(acc[4 * h + 1], p, a.r32, a.r32q, a.oneq);
-                        v.z = mod64_q(acc[4 * h + 2], p, a.r32, a.r32q, a.oneq);
-                        v.w = mod64_q(acc[4 * h + 3], p, a.r32, a.r32q, a.oneq);
-                        *reinterpret_cast<uint4 *>(dst + 4 * h) = v;
-                    }
-                continue;
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++) acc[u] = (u < cols) ? dst[u] : 0ull;
-            for (int b0 = 0; b0 < rank; b0 += 8) {
-                const int bend = b0 + 8 < rank ? b0 + 8 : rank;
-                for (int b = b0; b < bend; b++) {
-                    const uint64_t xv = S.X[ia][b];
-                    const uint32_t *src = base + S.pivrow[b] * width;
-#pragma unroll
-                    for (int u = 0; u < 8; u++)
-                        if (u < cols) acc[u] += xv * src[u];
-                }
-#pragma unroll
-                for (int u = 0; u < 8; u++) acc[u] = fold(acc[u], a.r32);
-            }
-#pragma unroll
-            for (int u = 0; u < 8; u++)
-                if (u < cols) dst[u] = mod64_q(acc[u], p, a.r32, a.r32q, a.oneq);
-        }
-        // growth test on this CTA's columns: a pivot row nonzero at coefficient alen-1
-        for (int idx = tid; idx < rank * cm; idx += nth) {
-            const int b = idx / cm, col = idx - b * cm;
-            if (AB[(size_t)(alen - 1) * sab + S.pivrow[b] * ncm + col] != 0) grow = 1;
-        }
-        grow = __syncthreads_or(grow);
-        if (tid == 0) growf0[c] = grow;
-        // 5b. pivot rows times x (one coefficient more than the length: it may grow)
-        const int nlen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
-        for (int idx = tid; idx < rank * (cm + cn); idx += nth) {
-            const int b = idx / (cm + cn), col = idx - b * (cm + cn);
-            const int row = S.pivrow[b];
-            if (col < cm) {
-                for (int d = nlen - 1; d > 0; d--)
-                    AB[(size_t)d * sab + row * ncm + col] = AB[(size_t)(d - 1) * sab + row * ncm + col];
-                AB[row * ncm + col] = 0;
-            } else {
-                const int j = col - cm;
-                for (int d = order - 1; d > ord; d--)
-                    R[(size_t)d * sr + row * ncn + j] = R[(size_t)(d - 1) * sr + row * ncn + j];
+                E0[(n0 + jl) * (LC_MAXM + 1) + r] = v;
             }
         }
-        if (tid < rank) S.sh[S.pivrow[tid]] += 1;
-        __syncthreads();
     }
+    if (c > 0 && pending)
+        lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, order - 1, tid, nth);
 
-    // output: columns of this CTA, entry-major; coefficients past the length are zero
-    const int olen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
-    for (int64_t idx = tid; idx < (int64_t)m * cm * a.ldo; idx += nth) {
-        const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
-        const int i = (int)(e / cm), il = (int)(e - (int64_t)i * cm);
-        a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < olen ? (uint64_t)AB[(size_t)d * sab + i * ncm + il] : 0ull;
+    // output: columns of this slice, entry-major; coefficients past the length are zero
+    if (c > 0) {
+        const int olen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
+        for (int64_t idx = tid; idx < (int64_t)m * cm * a.ldo; idx += nth) {
+            const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
+            const int i = (int)(e / cm), il = (int)(e - (int64_t)i * cm);
+            a.out[((int64_t)i * m + m0 + il) * a.ldo + d] = d < olen ? (uint64_t)AB[(size_t)d * sab + i * ncm + il] : 0ull;
+        }
     }
     if (c == 0 && tid < m) a.shift[tid] = S.sh[tid];
     cluster.sync();   // no CTA leaves while another may still address its shared memory
@@ -641,9 +724,51 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
 
 static size_t leaf_cluster_smem(int m, int n, int order)
 {
-    const int ncm = (m + LC_CL - 1) / LC_CL, ncn = (n + LC_CL - 1) / LC_CL;
+    const int ncm = (m + LC_SL - 1) / LC_SL, ncn = (n + LC_SL - 1) / LC_SL;
     const int pad = ((ncm & 3) == 0 && (ncn & 3) == 0) ? 4 : 1;   // as in the kernel
     return ((size_t)(order + 1) * (m * ncm + pad) + (size_t)order * (m * ncn + pad)) * sizeof(uint32_t);
+}
+
+// launch (or, with query, the number of co-resident clusters) of the cluster leaf:
+// LC_CL CTAs per cluster, a size given at launch because it is above the portable 8
+static cudaError_t leaf_cluster_launch(const LeafArgs &a, size_t smem, cudaStream_t st, bool query, int *nclusters)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(LC_CL, 1, 1);
+    cfg.blockDim = dim3(LC_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = LC_CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (query) return cudaOccupancyMaxActiveClusters(nclusters, mbasis_leaf_cluster_kernel, &cfg);
+    return cudaLaunchKernelEx(&cfg, mbasis_leaf_cluster_kernel, a);
+}
+
+// whether a cluster of LC_CL CTAs with the largest leaf's shared memory fits on the
+// device (checked once; otherwise the leaves run on the single-CTA kernel)
+static bool leaf_cluster_ready()
+{
+    static int state = 0;   // 0: not checked, 1: ready, -1: unavailable
+    if (state == 0) {
+        const size_t smax = leaf_cluster_smem(LC_MAXM, LC_MAXN, LC_MAXORD);
+        int nc = 0;
+        LeafArgs none{};
+        state = -1;
+        if (cudaFuncSetAttribute(mbasis_leaf_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+                cudaSuccess &&
+            cudaFuncSetAttribute(mbasis_leaf_cluster_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smax) ==
+                cudaSuccess &&
+            leaf_cluster_launch(none, smax, 0, true, &nc) == cudaSuccess && nc >= 1)
+            state = 1;
+        else
+            (void)cudaGetLastError();
+    }
+    return state == 1;
 }
 
 // ---------------------------------------------------------------------------
@@ -710,17 +835,10 @@ static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, i
         a.r2 = (uint32_t)h_mulmod(a.r32, a.r32, a.p);
     }
     pmlg_ctx *ctx = S.ctx;
-    const bool cluster = (a.p & 1u) && S.m <= LC_MAXM && S.n <= LC_MAXN && order <= LC_MAXORD;
+    const bool cluster = (a.p & 1u) && S.m <= LC_MAXM && S.n <= LC_MAXN && order <= LC_MAXORD && leaf_cluster_ready();
     if (cluster) {
-        const size_t smem = leaf_cluster_smem(a.m, a.n, a.order);
-        static size_t attr = 0;
-        if (smem > attr) {
-            PMLG_CUDA_TRY(cudaFuncSetAttribute(mbasis_leaf_cluster_kernel,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr = smem;
-        }
         prof_begin(ctx, "mbasis_leaf_cluster", S.st);
-        mbasis_leaf_cluster_kernel<<<LC_CL, LC_THREADS, smem, S.st>>>(a);
+        PMLG_CUDA_TRY(leaf_cluster_launch(a, leaf_cluster_smem(a.m, a.n, a.order), S.st, false, nullptr));
         prof_end(ctx, S.st);
     } else {
         prof_begin(ctx, "mbasis_leaf", S.st);

@@ -83,3 +83,22 @@ def test_pmbasis_config4_scaled(ctx):
     ref, rsh = oracle.pmbasis(F, 1024, [0] * 64, p, nthreads=16)
     assert sh == list(rsh)
     assert np.array_equal(ab, ref)
+
+
+def test_pmbasis_cluster_nonpivot_columns(ctx):
+    """64x32 inputs whose eliminations meet columns without a pivot before the
+    rank is full (zero and repeated rows of F, repeated columns): the cluster
+    leaf's look-ahead publication and its rebuilt pivot entries, bit-exact
+    against the oracle."""
+    p = P998
+    F = oracle.rand_poly_mat(64, 32, 96, p, 11)
+    F[3] = 0
+    F[40] = 0
+    F[17] = F[5]
+    F[:, 9] = F[:, 2]
+    F[:, 30] = (3 * F[:, 1]) % p
+    for shift in ([0] * 64, [(7 * i) % 13 for i in range(64)]):
+        ab, sh = _pm(ctx, F, 96, shift, p)
+        ref, rsh = oracle.pmbasis(F, 96, shift, p, nthreads=8)
+        assert sh == list(rsh)
+        assert np.array_equal(ab, ref)
