@@ -273,19 +273,21 @@ mbasis_leaf_kernel(LeafArgs a)
 // its own shared memory, the columns [q*ncm, (q+1)*ncm) of every coefficient of
 // appbas and the columns [q*ncn, (q+1)*ncn) of every coefficient of the residual
 // R = appbas * F mod x^order, which every row operation keeps up to date (so the
-// residual of step s is R[s]).  Each step s has two cluster barrier phases:
-//   G_s  the slice CTAs have written the permuted R[s]^T into CTA 0's shared
-//        memory (distributed shared memory stores);
-//   X_s  CTA 0 has published the pivots and X of step s, and the slice CTAs have
-//        finished the update of step s-1.
-// CTA 0, between G_s and X_s: the elimination of R[s]^T, then X.  The slice CTAs,
-// after X_s: take the pivots and X; add one to the pivot rows' shifts; compute
-// the stable shift permutation of step s+1 and the one coefficient s+1 of the
-// updated residual (pivot rows take their coefficient s, non-pivot rows add X
-// times the pivot rows), write it into CTA 0 and arrive at G_{s+1}; then apply
-// the whole update of step s to their slices while CTA 0 eliminates step s+1.
+// residual of step s is R[s]).  One cluster barrier phase Q_s per step: CTA 0 has
+// published the pivots and X of step s, and the slice CTAs have finished the
+// update of step s-1 and pushed the coefficients s+1 and s of their residual
+// slices (as they are before step s) into CTA 0's shared memory
+// (distributed shared memory stores).
 //
-// Elimination (CTA 0, its first LC_EW warps): lane j holds row j of E = R[s]^T
+// CTA 0, between Q_{s-1} and Q_s: the coefficient s of the residual after step
+// s-1 (pivot rows take their coefficient s-1, non-pivot rows add X times the
+// pivot rows), permuted and transposed into E = R[s]^T; the elimination of E;
+// the pivot inverses and X, while other warps shift the pivot rows' shifts and
+// compute the stable shift permutation of step s+1.  The slice CTAs, in the same
+// interval: the whole update of step s-1 on their slices.  So the elimination of
+// step s, the one chain that cannot be split, runs while the slice CTAs update.
+//
+// Elimination (CTA 0, its first LC_EW warps): lane j holds row j of E
 // (j < n <= 32), warp w holds columns [4w, 4w+4) in registers (LC_EW = 16 warps
 // of 4 columns by default); column c's owner warp finds the pivot with a ballot
 // and publishes it through shared memory (double-buffered, one barrier per
@@ -301,7 +303,7 @@ mbasis_leaf_kernel(LeafArgs a)
 // slice per thread) on appbas' coefficients d < alen and R's coefficients past s;
 // pivot rows times x.  The length of appbas grows by one when a pivot row reaches
 // its top coefficient (nmod_mat_poly_mbasis.c:306-313): each slice CTA reports it
-// into CTA 0, and every slice CTA reads the flags after X_{s+1}.
+// into CTA 0, and every slice CTA reads the flags after the next phase.
 
 constexpr int LC_SL = 8;                 // slice CTAs
 constexpr int LC_CL = 1 + LC_SL;         // cluster size (a non-portable size, above 8)
@@ -349,14 +351,15 @@ __device__ __forceinline__ void cluster_wait()
 
 struct LcShared
 {
-    uint32_t E[LC_MAXN][LC_MAXM + 1];   // CTA 0: gathered R[s]^T
-    uint32_t X[LC_MAXM][LC_MAXM];       // nullity x rank (CTA 0 computes it, the slice CTAs copy it)
-    int pivrow[LC_MAXM], nprow[LC_MAXM];
-    int rowidx[LC_MAXM];                // slice CTAs: row -> its non-pivot index, -1 for a pivot row
-    int info[2];                        // CTA 0: rank and nullity of the current step
+    uint32_t E[LC_MAXN][LC_MAXM + 1];   // CTA 0: R[s]^T, permuted
+    alignas(16) uint32_t X[2][LC_MAXM][LC_MAXN];   // CTA 0: X (nullity x rank) by step parity; slice CTAs: a copy in [0]
+    int pivrow[2][LC_MAXM], nprow[2][LC_MAXM];   // likewise
+    int info[2][2];                     // CTA 0: rank and nullity by step parity
+    int rowidx[LC_MAXM];                // CTA 0: row -> its non-pivot index in the last step, -1 for a pivot row
     int growf[2][LC_SL];                // CTA 0: per-slice growth flags, by step parity
-    long long sh[LC_MAXM];
-    int perm[LC_MAXM];
+    long long sh[LC_MAXM];              // CTA 0: shifts
+    int perm[LC_MAXM];                  // CTA 0: stable shift permutation of the current step
+    int pos[LC_MAXM];                   // CTA 0: its inverse (row -> rank)
     uint32_t fbuf[2][32];               // the current column's values, pivot value and
     uint32_t pvbuf[2];                  // pivot lane (double-buffered by column)
     int plbuf[2];
@@ -364,24 +367,22 @@ struct LcShared
     uint32_t inv[LC_MAXM];
 };
 
-// stable shift permutation (rank counting, 8 threads per row): perm[r] = the row of rank r
-// (_find_shift_permutation, nmod_mat_poly_mbasis.c:69-114)
-__device__ __forceinline__ void lc_perm(LcShared &S, int m, int tid)
+// stable shift permutation (rank counting, one thread per row t < m):
+// perm[r] = the row of rank r (_find_shift_permutation, nmod_mat_poly_mbasis.c:69-114)
+__device__ __forceinline__ void lc_perm(LcShared &S, int m, int t)
 {
-    const int i = tid >> 3, part = tid & 7;
-    int r = 0;
-    if (i < m) {
-        const long long v = S.sh[i];
-        for (int jj = part; jj < m; jj += 8) r += (S.sh[jj] < v) || (S.sh[jj] == v && jj < i);
+    if (t < m) {
+        const long long v = S.sh[t];
+        int r = 0;
+        for (int j = 0; j < m; j++) r += (S.sh[j] < v) || (S.sh[j] == v && j < t);
+        S.perm[r] = t;
+        S.pos[t] = r;
     }
-    r += __shfl_xor_sync(0xffffffffu, r, 1);
-    r += __shfl_xor_sync(0xffffffffu, r, 2);
-    r += __shfl_xor_sync(0xffffffffu, r, 4);
-    if (i < m && part == 0) S.perm[r] = i;
 }
 
-// CTA 0, step s: elimination of E = R[s]^T, pivots, X, and the shifts of the next
-// step.  S.perm holds the permutation of step s.  Ends with a block barrier.
+// CTA 0, step s: elimination of E = R[s]^T, pivots, X, the shifts of the next step
+// and its permutation.  S.perm holds the permutation of step s.  Ends with a block
+// barrier.
 __device__ void lc_eliminate(LcShared &S, const LeafArgs &a, int s, int tid, int nth)
 {
     const int m = a.m, n = a.n;
@@ -439,29 +440,43 @@ __device__ void lc_eliminate(LcShared &S, const LeafArgs &a, int s, int tid, int
         for (int k = 0; k < LC_CPW; k++)
             if (lane < n && LC_CPW * w + k < m) S.E[lane][LC_CPW * w + k] = x[k];
     }
-    if (tid == 0) S.info[0] = rank;
+    if (tid == 0) S.info[s & 1][0] = rank;
     __syncthreads();
-    rank = S.info[0];
+    rank = S.info[s & 1][0];
     const int nullity = m - rank;
-    if (tid < rank) S.pivrow[tid] = S.perm[S.pivcol[tid]];
-    if (tid < nullity) S.nprow[tid] = S.perm[S.nonpiv[tid]];
+    const int par = s & 1;
+    if (tid < rank) S.pivrow[par][tid] = S.perm[S.pivcol[tid]];
+    if (tid < nullity) S.nprow[par][tid] = S.perm[S.nonpiv[tid]];
+    if (tid == 0) S.info[par][1] = nullity;
+    __syncthreads();
+    // warp 0: pivot inverses; warps 2-3: shifts and permutation of the next step;
+    // warps 4-5: row -> non-pivot index
+    if (tid < 32) {
+        if (tid < rank && nullity > 0)
+            S.inv[tid] = mont_pow(S.E[S.pivlane[tid]][S.pivcol[tid]], p - 2, p, a.pneg, a.r2, a.r32);
+    } else if (tid >= 64 && tid < 128) {
+        const int t = tid - 64;
+        if (nullity == 0) {
+            if (t < m) S.sh[t] += a.order - s;
+        } else {
+            if (t < rank) S.sh[S.pivrow[par][t]] += 1;
+            asm volatile("bar.sync 2, 64;" ::: "memory");
+            lc_perm(S, m, t);
+        }
+    } else if (tid >= 128 && tid < 192) {
+        const int t = tid - 128;
+        if (t < m) S.rowidx[t] = -1;
+        asm volatile("bar.sync 3, 64;" ::: "memory");
+        if (t < nullity) S.rowidx[S.nprow[par][t]] = t;
+    }
+    __syncthreads();
     if (rank > 0 && nullity > 0) {
-        if (tid < rank) S.inv[tid] = mont_pow(S.E[S.pivlane[tid]][S.pivcol[tid]], p - 2, p, a.pneg, a.r2, a.r32);
-        __syncthreads();
         for (int idx = tid; idx < nullity * rank; idx += nth) {
             const int ia = idx / rank, b = idx - ia * rank;
             const uint32_t v = mod64_q((uint64_t)S.E[S.pivlane[b]][S.nonpiv[ia]] * S.inv[b], p,
                                        a.r32, a.r32q, a.oneq);
-            S.X[ia][b] = v ? p - v : 0u;
+            S.X[par][ia][b] = v ? p - v : 0u;
         }
-    }
-    __syncthreads();
-    // shifts of the next step: pivot rows + 1; with no nullity, every row + (order - s)
-    if (tid == 0) S.info[1] = nullity;
-    if (nullity == 0) {
-        if (tid < m) S.sh[tid] += a.order - s;
-    } else if (tid < rank) {
-        S.sh[S.pivrow[tid]] += 1;
     }
     __syncthreads();
 }
@@ -484,7 +499,7 @@ __device__ int lc_update(LcShared &S, const LeafArgs &a, uint32_t *AB, uint32_t 
         const int d = isab ? j2 - ia * per : s + 1 + (j2 - ia * per);
         const int width = isab ? ncm : ncn, cols = isab ? cm : cn;
         uint32_t *base = isab ? AB + (size_t)d * sab : R + (size_t)d * sr;
-        uint32_t *dst = base + S.nprow[ia] * width;
+        uint32_t *dst = base + S.nprow[0][ia] * width;
         uint64_t acc[8];
         if (vec) {
             // whole rows of 4 or 8 words (columns past `cols` are zero padding)
@@ -500,8 +515,8 @@ __device__ int lc_update(LcShared &S, const LeafArgs &a, uint32_t *AB, uint32_t 
             for (int b0 = 0; b0 < rank; b0 += 8) {
                 const int bend = b0 + 8 < rank ? b0 + 8 : rank;
                 for (int b = b0; b < bend; b++) {
-                    const uint64_t xv = S.X[ia][b];
-                    const uint32_t *src = base + S.pivrow[b] * width;
+                    const uint64_t xv = S.X[0][ia][b];
+                    const uint32_t *src = base + S.pivrow[0][b] * width;
 #pragma unroll
                     for (int h = 0; h < 2; h++)
                         if (h < nq) {
@@ -530,8 +545,8 @@ __device__ int lc_update(LcShared &S, const LeafArgs &a, uint32_t *AB, uint32_t 
         for (int b0 = 0; b0 < rank; b0 += 8) {
             const int bend = b0 + 8 < rank ? b0 + 8 : rank;
             for (int b = b0; b < bend; b++) {
-                const uint64_t xv = S.X[ia][b];
-                const uint32_t *src = base + S.pivrow[b] * width;
+                const uint64_t xv = S.X[0][ia][b];
+                const uint32_t *src = base + S.pivrow[0][b] * width;
 #pragma unroll
                 for (int u = 0; u < 8; u++)
                     if (u < cols) acc[u] += xv * src[u];
@@ -547,14 +562,14 @@ __device__ int lc_update(LcShared &S, const LeafArgs &a, uint32_t *AB, uint32_t 
     int grow = 0;
     for (int idx = tid; idx < rank * cm; idx += nth) {
         const int b = idx / cm, col = idx - b * cm;
-        if (AB[(size_t)(alen - 1) * sab + S.pivrow[b] * ncm + col] != 0) grow = 1;
+        if (AB[(size_t)(alen - 1) * sab + S.pivrow[0][b] * ncm + col] != 0) grow = 1;
     }
     grow = __syncthreads_or(grow);
     // pivot rows times x (one coefficient more than the length: it may grow)
     const int nlen = alen + 1 <= order + 1 ? alen + 1 : order + 1;
     for (int idx = tid; idx < rank * (cm + cn); idx += nth) {
         const int b = idx / (cm + cn), col = idx - b * (cm + cn);
-        const int row = S.pivrow[b];
+        const int row = S.pivrow[0][b];
         if (col < cm) {
             for (int d = nlen - 1; d > 0; d--)
                 AB[(size_t)d * sab + row * ncm + col] = AB[(size_t)(d - 1) * sab + row * ncm + col];
@@ -608,103 +623,126 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         }
     }
     if (tid < m) S.sh[tid] = a.shift[tid];
-    uint32_t *E0 = cluster.map_shared_rank(&S.E[0][0], 0);
+    // CTA 0's dynamic shared memory: by step parity, the coefficients s and s-1 of the
+    // residual before step s-1, [2][2][m][n]
+    uint32_t *D0 = cluster.map_shared_rank(dyn, 0);
     int *growf0 = cluster.map_shared_rank(&S.growf[0][0], 0);
     int alen = 1;              // exact length of appbas (slice CTAs)
     cluster.sync();            // every CTA runs before distributed shared memory is addressed
 
     if (c > 0) {
-        // R[0]^T, permuted, into CTA 0
-        lc_perm(S, m, tid);
-        __syncthreads();
-        for (int idx = tid; idx < m * cn; idx += nth) {
-            const int r = idx / cn, jl = idx - r * cn;
-            E0[(n0 + jl) * (LC_MAXM + 1) + r] = R[S.perm[r] * ncn + jl];
+        for (int idx = tid; idx < m * cn; idx += nth) {   // R[0] into CTA 0
+            const int i = idx / cn, jl = idx - i * cn;
+            D0[i * n + n0 + jl] = R[i * ncn + jl];
         }
+    } else {
+        if (tid < m) lc_perm(S, m, tid);
     }
+    cluster_arrive();
+    cluster_wait();
+
     bool pending = false;      // slice CTAs: the update of the previous step is still to apply
     int prank = 0, pnull = 0;  // its rank and nullity
     for (int s = 0; s < order; s++) {
         if (c == 0) {
-            lc_perm(S, m, tid);
-            cluster_arrive();
-            cluster_wait();                              // G_s
+            // coefficient s of the residual after step s-1, permuted and transposed into E
+            const uint32_t *Dc = dyn + (size_t)((s & 1) * 2) * m * n;     // coefficient s
+            const uint32_t *Dp = Dc + (size_t)m * n;                       // coefficient s-1
+            const int q1 = (s - 1) & 1;
+            const int prk = s > 0 ? S.info[q1][0] : 0, pnl = m - prk;
+            if (prk == 0) {
+                for (int idx = tid; idx < m * n; idx += nth) {
+                    const int i = idx / n, j = idx - i * n;
+                    S.E[j][S.pos[i]] = Dc[idx];
+                }
+            } else {
+                // pivot rows of step s-1 were multiplied by x: they take their coefficient s-1
+                for (int idx = tid; idx < prk * n; idx += nth) {
+                    const int b = idx / n, j = idx - b * n, i = S.pivrow[q1][b];
+                    S.E[j][S.pos[i]] = Dp[i * n + j];
+                }
+                // non-pivot rows a and a+16 per warp, a lane per column: += X[a][.] * pivot rows,
+                // X read 4 entries at a time
+                const int w = tid >> 5, lane = tid & 31;
+                if (lane < n) {
+                    for (int a0 = w; a0 < pnl; a0 += 2 * (LC_THREADS / 32)) {
+                        const int a1 = a0 + LC_THREADS / 32;
+                        const bool two = a1 < pnl;
+                        const int i0 = S.nprow[q1][a0], i1 = two ? S.nprow[q1][a1] : i0;
+                        uint64_t acc0 = Dc[i0 * n + lane], acc1 = Dc[i1 * n + lane];
+                        for (int b0 = 0; b0 < prk; b0 += 4) {
+                            const uint4 x0 = *reinterpret_cast<const uint4 *>(&S.X[q1][a0][b0]);
+                            const uint4 x1 = *reinterpret_cast<const uint4 *>(&S.X[q1][two ? a1 : a0][b0]);
+                            uint64_t d[4];
+#pragma unroll
+                            for (int k = 0; k < 4; k++)
+                                d[k] = b0 + k < prk ? Dc[S.pivrow[q1][b0 + k] * n + lane] : 0u;
+                            acc0 += x0.x * d[0] + x0.y * d[1] + x0.z * d[2] + x0.w * d[3];
+                            acc1 += x1.x * d[0] + x1.y * d[1] + x1.z * d[2] + x1.w * d[3];
+                            if ((b0 & 7) == 4 || b0 + 4 >= prk) {
+                                acc0 = fold(acc0, a.r32);
+                                acc1 = fold(acc1, a.r32);
+                            }
+                        }
+                        S.E[lane][S.pos[i0]] = mod64_q(acc0, p, a.r32, a.r32q, a.oneq);
+                        if (two) S.E[lane][S.pos[i1]] = mod64_q(acc1, p, a.r32, a.r32q, a.oneq);
+                    }
+                }
+            }
+            __syncthreads();
             lc_eliminate(S, a, s, tid, nth);
             cluster_arrive();
-            cluster_wait();                              // X_s
-            if (S.info[1] == 0) break;
+            cluster_wait();                              // Q_s
+            if (S.info[s & 1][1] == 0) break;
             continue;
         }
-        cluster_arrive();                                // G_s: this CTA's part of R[s]^T is in CTA 0
         int grow = 0;
         if (pending) grow = lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, s - 1, tid, nth);
         if (pending && tid == 0) growf0[((s - 1) & 1) * LC_SL + q] = grow;
-        cluster_wait();
+        if (s + 1 < order) {
+            // coefficients s+1 and s of this slice, as they are before step s, into CTA 0
+            uint32_t *Db = D0 + (size_t)(((s + 1) & 1) * 2) * m * n;
+            for (int idx = tid; idx < m * cn; idx += nth) {
+                const int i = idx / cn, jl = idx - i * cn;
+                Db[i * n + n0 + jl] = R[(size_t)(s + 1) * sr + i * ncn + jl];
+                Db[(size_t)m * n + i * n + n0 + jl] = R[(size_t)s * sr + i * ncn + jl];
+            }
+        }
         cluster_arrive();
-        cluster_wait();                                  // X_s
+        cluster_wait();                                  // Q_s
         // the growth of step s-1 in any slice, then rank, pivots and X of step s
         if (pending)
             alen += __syncthreads_or(tid < LC_SL ? growf0[((s - 1) & 1) * LC_SL + tid] : 0);
-        const int *info0 = cluster.map_shared_rank(S.info, 0);
+        const int par = s & 1;
+        const int *info0 = cluster.map_shared_rank(&S.info[par][0], 0);
         const int rank = info0[0], nullity = info0[1];
         if (nullity == 0) {
-            // appbas = x^(order-s) * appbas, shift += order - s (nmod_mat_poly_mbasis.c:221-259)
+            // appbas = x^(order-s) * appbas (nmod_mat_poly_mbasis.c:221-259)
             const int k = order - s;
             for (int idx = tid; idx < m * ncm; idx += nth) {
                 for (int d = alen - 1; d >= 0; d--) AB[((size_t)(d + k)) * sab + idx] = AB[(size_t)d * sab + idx];
                 for (int d = 0; d < k; d++) AB[(size_t)d * sab + idx] = 0;
             }
-            if (tid < m) S.sh[tid] += k;
             alen += k;
             pending = false;
             __syncthreads();
             break;
         }
         if (rank > 0) {
-            const int *pr0 = cluster.map_shared_rank(S.pivrow, 0);
-            const int *np0 = cluster.map_shared_rank(S.nprow, 0);
-            const uint32_t *X0 = cluster.map_shared_rank(&S.X[0][0], 0);
-            if (tid < rank) S.pivrow[tid] = pr0[tid];
-            if (tid < nullity) S.nprow[tid] = np0[tid];
+            const int *pr0 = cluster.map_shared_rank(&S.pivrow[par][0], 0);
+            const int *np0 = cluster.map_shared_rank(&S.nprow[par][0], 0);
+            const uint32_t *X0 = cluster.map_shared_rank(&S.X[par][0][0], 0);
+            if (tid < rank) S.pivrow[0][tid] = pr0[tid];
+            if (tid < nullity) S.nprow[0][tid] = np0[tid];
             for (int idx = tid; idx < nullity * rank; idx += nth) {
                 const int ia = idx / rank, b = idx - ia * rank;
-                S.X[ia][b] = X0[ia * LC_MAXM + b];
+                S.X[0][ia][b] = X0[ia * LC_MAXN + b];
             }
             __syncthreads();
-            if (tid < m) S.rowidx[tid] = -1;
-            if (tid < rank) S.sh[S.pivrow[tid]] += 1;
-            __syncthreads();
-            if (tid < nullity) S.rowidx[S.nprow[tid]] = tid;
         }
         pending = rank > 0;
         prank = rank;
         pnull = nullity;
-        if (s + 1 < order) {
-            // coefficient s+1 of the residual after step s, permuted and transposed, into CTA 0
-            lc_perm(S, m, tid);
-            __syncthreads();
-            for (int idx = tid; idx < m * cn; idx += nth) {
-                const int r = idx / cn, jl = idx - r * cn;
-                const int i = S.perm[r];
-                const uint32_t *Rn = R + (size_t)(s + 1) * sr;
-                uint32_t v;
-                const int ia = rank > 0 ? S.rowidx[i] : 0;
-                if (rank == 0) {
-                    v = Rn[i * ncn + jl];
-                } else if (ia < 0) {
-                    v = R[(size_t)s * sr + i * ncn + jl];          // pivot row times x
-                } else {
-                    uint64_t acc = Rn[i * ncn + jl];
-                    for (int b0 = 0; b0 < rank; b0 += 8) {
-                        const int bend = b0 + 8 < rank ? b0 + 8 : rank;
-                        for (int b = b0; b < bend; b++) acc += (uint64_t)S.X[ia][b] * Rn[S.pivrow[b] * ncn + jl];
-                        acc = fold(acc, a.r32);
-                    }
-                    v = mod64_q(acc, p, a.r32, a.r32q, a.oneq);
-                }
-                E0[(n0 + jl) * (LC_MAXM + 1) + r] = v;
-            }
-        }
     }
     if (c > 0 && pending)
         lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, order - 1, tid, nth);
@@ -726,7 +764,9 @@ static size_t leaf_cluster_smem(int m, int n, int order)
 {
     const int ncm = (m + LC_SL - 1) / LC_SL, ncn = (n + LC_SL - 1) / LC_SL;
     const int pad = ((ncm & 3) == 0 && (ncn & 3) == 0) ? 4 : 1;   // as in the kernel
-    return ((size_t)(order + 1) * (m * ncm + pad) + (size_t)order * (m * ncn + pad)) * sizeof(uint32_t);
+    const size_t slices = ((size_t)(order + 1) * (m * ncm + pad) + (size_t)order * (m * ncn + pad)) * sizeof(uint32_t);
+    const size_t coeffs = (size_t)4 * m * n * sizeof(uint32_t);   // CTA 0: [2][2][m][n]
+    return slices > coeffs ? slices : coeffs;
 }
 
 // launch (or, with query, the number of co-resident clusters) of the cluster leaf:
