@@ -102,3 +102,21 @@ def test_pmbasis_cluster_nonpivot_columns(ctx):
         ref, rsh = oracle.pmbasis(F, 96, shift, p, nthreads=8)
         assert sh == list(rsh)
         assert np.array_equal(ab, ref)
+
+
+@pytest.mark.parametrize("dims", [(64, 4, 64), (48, 20, 80), (33, 31, 40), (64, 1, 48), (8, 32, 40),
+                                  (64, 32, 64), (17, 9, 70)])
+def test_pmbasis_cluster_shapes(ctx, dims):
+    """Shapes at and inside the cluster leaf's limits (m <= 64, n <= 32): large
+    nullity (several non-pivot row groups per warp when the eliminator forms the
+    next residual coefficient), slices whose widths are not multiples of 4 (the
+    word-wise update), n = 1, and m < n (nullity 0: appbas times a power of x),
+    each with a zero, an increasing and a hermite-like shift."""
+    m, n, order = dims
+    p = P998
+    F = oracle.rand_poly_mat(m, n, order, p, 500 + m + n)
+    for shift in ([0] * m, list(range(m)), [order * (m - i) for i in range(m)]):
+        ab, sh = _pm(ctx, F, order, shift, p)
+        ref, rsh = oracle.pmbasis(F, order, shift, p, nthreads=8)
+        assert sh == list(rsh)
+        assert np.array_equal(ab, ref)
