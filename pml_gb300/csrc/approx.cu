@@ -42,6 +42,7 @@ struct LeafArgs
     uint32_t pneg;    // -p^{-1} mod 2^32 (Montgomery reduction)
     uint32_t r2;      // 2^64 mod p (Montgomery conversion)
     int *err;         // device error word: a bounded wait gave up
+    unsigned long long *len_out;   // device: a bound on appbas' length (exact unless rows cancel)
 };
 
 __device__ __forceinline__ uint32_t mulmod32(uint32_t a, uint32_t b, const LeafArgs &A)
@@ -262,6 +263,7 @@ mbasis_leaf_kernel(LeafArgs a)
         a.out[idx] = d < alen ? (uint64_t)a.AB[d * m * m + e] : 0ull;
     }
     if (tid < m) a.shift[tid] = sh[tid];
+    if (tid == 0) *a.len_out = (unsigned long long)alen;
 }
 
 // ---------------------------------------------------------------------------
@@ -744,8 +746,18 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
         prank = rank;
         pnull = nullity;
     }
-    if (c > 0 && pending)
-        lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, order - 1, tid, nth);
+    if (c > 0 && pending) {
+        const int grow = lc_update(S, a, AB, R, sab, sr, ncm, ncn, cm, cn, vec, prank, pnull, alen, order - 1, tid, nth);
+        if (tid == 0) growf0[((order - 1) & 1) * LC_SL + q] = grow;
+    }
+    // the length of appbas: alen, plus one when a pivot row of the last step reached the
+    // top coefficient in any slice (pending is the same in every slice CTA)
+    cluster.sync();
+    if (c == 1) {
+        int g = 0;
+        if (pending) g = __syncthreads_or(tid < LC_SL ? growf0[((order - 1) & 1) * LC_SL + tid] : 0);
+        if (tid == 0) *a.len_out = (unsigned long long)(alen + g <= order + 1 ? alen + g : order + 1);
+    }
 
     // output: columns of this slice, entry-major; coefficients past the length are zero
     if (c > 0) {
@@ -863,6 +875,7 @@ static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, i
     a.R = R; a.AB = AB;
     a.shift = S.d_shift;
     a.err = S.ctx->d_err;
+    a.len_out = S.d_tmp;
     a.m = (int)S.m; a.n = (int)S.n; a.order = (int)order;
     a.p = (uint32_t)S.p;
     a.r32 = (uint32_t)((1ull << 32) % S.p);
@@ -920,7 +933,11 @@ static int pmbasis_rec(PmState &S, uint64_t *appbas, int64_t ldA, const uint64_t
     const int64_t pl = flen < order ? flen : order;   // set_trunc(F, order)
     if (order <= S.leaf) {
         PMLG_TRY(leaf_run(S, appbas, ldA, F, ldF, pl, order));
-        return device_max_length(ctx, appbas, m * m, ldA, ldA, S.d_tmp, len, S.st);
+        unsigned long long h = 0;
+        PMLG_CUDA_TRY(cudaMemcpyAsync(&h, S.d_tmp, sizeof(h), cudaMemcpyDeviceToHost, S.st));
+        PMLG_CUDA_TRY(cudaStreamSynchronize(S.st));
+        *len = (int64_t)h;
+        return PMLG_OK;
     }
     const int64_t o1 = order >> 1, o2 = order - o1;
     const size_t mark = S.ar.top;
@@ -958,9 +975,13 @@ static int pmbasis_rec(PmState &S, uint64_t *appbas, int64_t ldA, const uint64_t
         j.lg = lg_for(j.cnt > 0 ? l1 + l2 - 1 : 1);
         j.p = S.p;
         PMLG_TRY(run_product(S, j));
+        // a bound on the product's length (exact unless the leading coefficients cancel):
+        // the products above size their transforms by it, and coefficients past the true
+        // length are zero; the entry point measures the exact length once at the end
+        *len = j.cnt;
     }
     S.ar.top = mark;
-    return device_max_length(ctx, appbas, m * m, ldA, ldA, S.d_tmp, len, S.st);
+    return PMLG_OK;
 }
 
 static int approx_entry(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *shift, const uint64_t *F,
@@ -999,6 +1020,7 @@ static int approx_entry(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *s
         len = 1;
     } else {
         PMLG_TRY(pmbasis_rec(S, appbas, cap, F, flen, flen, order, &len));
+        PMLG_TRY(device_max_length(ctx, appbas, m * m, cap, len, S.d_tmp, &len, st));   // exact
     }
     PMLG_CUDA_TRY(cudaMemcpyAsync(shift, S.d_shift, (size_t)m * 8, cudaMemcpyDeviceToHost, st));
     PMLG_TRY(device_status(ctx, st));
