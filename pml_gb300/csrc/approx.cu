@@ -367,6 +367,7 @@ struct LcShared
     int plbuf[2];
     int pivlane[LC_MAXM], pivcol[LC_MAXM], nonpiv[LC_MAXM];
     uint32_t inv[LC_MAXM];
+    alignas(16) uint32_t dpiv[LC_MAXN][LC_MAXN];   // CTA 0: the pivot rows of the last step, gathered
 };
 
 // stable shift permutation (rank counting, one thread per row t < m):
@@ -663,6 +664,12 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
                     const int b = idx / n, j = idx - b * n, i = S.pivrow[q1][b];
                     S.E[j][S.pos[i]] = Dp[i * n + j];
                 }
+                // the pivot rows' coefficient s, gathered in pivot order
+                for (int idx = tid; idx < prk * n; idx += nth) {
+                    const int b = idx / n, j = idx - b * n;
+                    S.dpiv[b][j] = Dc[S.pivrow[q1][b] * n + j];
+                }
+                __syncthreads();
                 // non-pivot rows a and a+16 per warp, a lane per column: += X[a][.] * pivot rows,
                 // X read 4 entries at a time
                 const int w = tid >> 5, lane = tid & 31;
@@ -672,22 +679,26 @@ mbasis_leaf_cluster_kernel(LeafArgs a)
                         const bool two = a1 < pnl;
                         const int i0 = S.nprow[q1][a0], i1 = two ? S.nprow[q1][a1] : i0;
                         uint64_t acc0 = Dc[i0 * n + lane], acc1 = Dc[i1 * n + lane];
-                        for (int b0 = 0; b0 < prk; b0 += 4) {
+                        uint64_t accb0 = 0, accb1 = 0;
+                        for (int b0 = 0; b0 < prk; b0 += 8) {
                             const uint4 x0 = *reinterpret_cast<const uint4 *>(&S.X[q1][a0][b0]);
                             const uint4 x1 = *reinterpret_cast<const uint4 *>(&S.X[q1][two ? a1 : a0][b0]);
-                            uint64_t d[4];
+                            const uint4 y0 = *reinterpret_cast<const uint4 *>(&S.X[q1][a0][b0 + 4]);
+                            const uint4 y1 = *reinterpret_cast<const uint4 *>(&S.X[q1][two ? a1 : a0][b0 + 4]);
+                            uint64_t d[8];
 #pragma unroll
-                            for (int k = 0; k < 4; k++)
-                                d[k] = b0 + k < prk ? Dc[S.pivrow[q1][b0 + k] * n + lane] : 0u;
+                            for (int k = 0; k < 8; k++) d[k] = b0 + k < prk ? S.dpiv[b0 + k][lane] : 0u;
                             acc0 += x0.x * d[0] + x0.y * d[1] + x0.z * d[2] + x0.w * d[3];
+                            accb0 += y0.x * d[4] + y0.y * d[5] + y0.z * d[6] + y0.w * d[7];
                             acc1 += x1.x * d[0] + x1.y * d[1] + x1.z * d[2] + x1.w * d[3];
-                            if ((b0 & 7) == 4 || b0 + 4 >= prk) {
-                                acc0 = fold(acc0, a.r32);
-                                acc1 = fold(acc1, a.r32);
-                            }
+                            accb1 += y1.x * d[4] + y1.y * d[5] + y1.z * d[6] + y1.w * d[7];
+                            acc0 = fold(acc0, a.r32);
+                            acc1 = fold(acc1, a.r32);
+                            accb0 = fold(accb0, a.r32);
+                            accb1 = fold(accb1, a.r32);
                         }
-                        S.E[lane][S.pos[i0]] = mod64_q(acc0, p, a.r32, a.r32q, a.oneq);
-                        if (two) S.E[lane][S.pos[i1]] = mod64_q(acc1, p, a.r32, a.r32q, a.oneq);
+                        S.E[lane][S.pos[i0]] = mod64_q(acc0 + accb0, p, a.r32, a.r32q, a.oneq);
+                        if (two) S.E[lane][S.pos[i1]] = mod64_q(acc1 + accb1, p, a.r32, a.r32q, a.oneq);
                     }
                 }
             }
