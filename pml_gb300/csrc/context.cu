@@ -386,6 +386,8 @@ PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
         if (ctx->bstream[i]) cudaStreamDestroy(ctx->bstream[i]);
     for (int i = 0; i <= pmlg_ctx::kBatchStreams; i++)
         if (ctx->bevent[i]) cudaEventDestroy(ctx->bevent[i]);
+    for (int i = 0; i < pmlg_ctx::kHostEvents; i++)
+        if (ctx->hevent[i]) cudaEventDestroy(ctx->hevent[i]);
     if (ctx->d_err) cudaFree(ctx->d_err);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     for (auto &r : ctx->prof) { cudaEventDestroy(r.beg); cudaEventDestroy(r.end); }

@@ -136,6 +136,9 @@ struct pmlg_ctx
     static constexpr int kBatchStreams = 8;
     cudaStream_t bstream[kBatchStreams] = {};
     cudaEvent_t bevent[kBatchStreams + 1] = {};
+    // events of the host-buffer product's copy/compute pipeline
+    static constexpr int kHostEvents = 16;
+    cudaEvent_t hevent[kHostEvents] = {};
     pmlg::Workspace ws_batch;      // per-stream scratch of the batched products
     // cached NTT tables
     static constexpr int kMaxTables = 256;

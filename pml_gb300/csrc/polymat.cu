@@ -59,11 +59,12 @@ static int product_bufs(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan,
     return PMLG_OK;
 }
 
-// forward transforms of A (which = 0) or B (which = 1)
+// forward transforms of the entries [e0, e1) of A (which = 0) or B (which = 1)
 static int product_forward(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, const ProductBufs &b,
-                           int which, cudaStream_t st)
+                           int which, int64_t e0, int64_t e1, cudaStream_t st)
 {
     const int64_t N = 1ll << j.lg;
+    if (e1 <= e0) return PMLG_OK;
     NttFwdArgs fa{};
     fa.lg = j.lg;
     fa.t = plan.t;
@@ -71,27 +72,29 @@ static int product_forward(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &pl
     for (int i = 0; i < plan.t; i++) fa.tab[i] = ntt_dev(b.tabs[i], false);
     if (which == 0) {
         const int64_t nA = j.r * j.k;
-        fa.in = j.A; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = nA;
-        fa.out = b.EA; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
+        fa.in = j.A + e0 * j.lda; fa.in_ld = j.lda; fa.in_off = j.a_off; fa.L = j.a_len; fa.nent = e1 - e0;
+        fa.out = b.EA + e0 * kPtTile; fa.prime_stride = N * nA; fa.tile_stride = kPtTile * nA;
     } else {
         const int64_t nB = j.k * j.c;
-        fa.in = j.B; fa.in_ld = j.ldb; fa.in_off = j.b_off; fa.L = j.b_len; fa.nent = nB;
-        fa.out = b.EB; fa.prime_stride = N * nB; fa.tile_stride = kPtTile * nB;
+        fa.in = j.B + e0 * j.ldb; fa.in_ld = j.ldb; fa.in_off = j.b_off; fa.L = j.b_len; fa.nent = e1 - e0;
+        fa.out = b.EB + e0 * kPtTile; fa.prime_stride = N * nB; fa.tile_stride = kPtTile * nB;
     }
     return ntt_forward(ctx, fa, st);
 }
 
-// pointwise products, one prime at a time (scaled by 1/N for the inverse transform)
+// pointwise products of the rows [i0, i1) of A and C, one prime at a time (scaled by
+// 1/N for the inverse transform)
 static int product_pointwise(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, const ProductBufs &b,
-                             int form, cudaStream_t st)
+                             int64_t i0, int64_t i1, int form, cudaStream_t st)
 {
     const int64_t N = 1ll << j.lg;
     const int64_t nA = j.r * j.k, nB = j.k * j.c, nC = j.r * j.c;
+    if (i1 <= i0) return PMLG_OK;
     for (int i = 0; i < plan.t; i++) {
         PwArgs pa{};
-        pa.A = {b.EA + (size_t)i * N * nA, kPtTile * nA, j.k};
+        pa.A = {b.EA + (size_t)i * N * nA + i0 * j.k * kPtTile, kPtTile * nA, j.k};
         pa.B = {b.EB + (size_t)i * N * nB, kPtTile * nB, j.c};
-        pa.C = b.EC + (size_t)i * N * nC;
+        pa.C = b.EC + (size_t)i * N * nC + i0 * j.c * kPtTile;
         pa.s_tile_c = kPtTile * nC;
         pa.ldc = j.c;
         pa.pt_tile = kPtTile;
@@ -100,7 +103,7 @@ static int product_pointwise(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &
         pa.npts = N;
         pa.accumulate = 0;
         pointwise_set_modulus(pa, plan.q[i], b.tabs[i]->ninv);   // the 1/N of the inverse transform
-        PMLG_TRY(pointwise_blocked(ctx, pa, j.r, j.k, j.c, form, st));
+        PMLG_TRY(pointwise_blocked(ctx, pa, i1 - i0, j.k, j.c, form, st));
     }
     return PMLG_OK;
 }
@@ -130,9 +133,9 @@ int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *s
 {
     ProductBufs b;
     PMLG_TRY(product_bufs(ctx, j, plan, scratch, b));
-    PMLG_TRY(product_forward(ctx, j, plan, b, 0, st));
-    PMLG_TRY(product_forward(ctx, j, plan, b, 1, st));
-    PMLG_TRY(product_pointwise(ctx, j, plan, b, form, st));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 0, 0, j.r * j.k, st));
+    PMLG_TRY(product_forward(ctx, j, plan, b, 1, 0, j.k * j.c, st));
+    PMLG_TRY(product_pointwise(ctx, j, plan, b, 0, j.r, form, st));
     return product_inverse(ctx, j, plan, b, 0, j.r * j.c, st);
 }
 
@@ -244,6 +247,8 @@ static int ensure_side_streams(pmlg_ctx *ctx, int nstreams)
         if (!ctx->bstream[s]) PMLG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->bstream[s], cudaStreamNonBlocking));
     for (int s = 0; s <= pmlg_ctx::kBatchStreams; s++)
         if (!ctx->bevent[s]) PMLG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->bevent[s], cudaEventDisableTiming));
+    for (int s = 0; s < pmlg_ctx::kHostEvents; s++)
+        if (!ctx->hevent[s]) PMLG_CUDA_TRY(cudaEventCreateWithFlags(&ctx->hevent[s], cudaEventDisableTiming));
     return PMLG_OK;
 }
 
@@ -390,33 +395,52 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
     PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan)));
     ProductBufs b;
     PMLG_TRY(product_bufs(ctx, j, plan, ctx->ws.ptr, b));
-    PMLG_TRY(ensure_side_streams(ctx, 1));
-    // Copies overlap the transforms: B is copied (side stream) while A is
-    // transformed, and C goes back in entry chunks while the later chunks
-    // are still being transformed back.
-    cudaStream_t cs = ctx->bstream[0];
-    cudaEvent_t *ev = ctx->bevent;
-    PMLG_CUDA_TRY(cudaEventRecord(ev[0], st));
-    PMLG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[0], 0));
-    PMLG_TRY(h2d(ctx, dA, A, bA, st));
-    PMLG_TRY(product_forward(ctx, j, plan, b, 0, st));
-    PMLG_TRY(h2d(ctx, dB, B, bB, cs));
-    PMLG_TRY(product_forward(ctx, j, plan, b, 1, cs));
-    PMLG_CUDA_TRY(cudaEventRecord(ev[1], cs));
-    PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ev[1], 0));
-    PMLG_TRY(product_pointwise(ctx, j, plan, b, ctx->form, st));
-    const int64_t nC = r * c;
-    const int nchunk = plan.direct && nC >= 4 ? 4 : 1;
-    for (int i = 0; i < nchunk; i++) {
-        const int64_t e0 = nC * i / nchunk, e1 = nC * (i + 1) / nchunk;
-        PMLG_TRY(product_inverse(ctx, j, plan, b, e0, e1, st));
-        PMLG_CUDA_TRY(cudaEventRecord(ev[2 + i], st));
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(cs, ev[2 + i], 0));
-        PMLG_CUDA_TRY(cudaMemcpyAsync(C + e0 * clen, dC + e0 * clen, (size_t)((e1 - e0) * clen) * 8,
-                                      cudaMemcpyDeviceToHost, cs));
+    PMLG_TRY(ensure_side_streams(ctx, 2));
+    // The link carries about 210 GB/s to the device and 193 GB/s back, 338 GB/s
+    // both ways at once, so the copies in the two directions are made to overlap:
+    // B goes first (its transforms follow its chunks), then A in row blocks; each
+    // row block of C is transformed, multiplied and transformed back as soon as
+    // its rows of A are in, and copied back while the next rows of A arrive.
+    cudaStream_t hs = ctx->bstream[0], ds = ctx->bstream[1];
+    cudaEvent_t *ev = ctx->hevent;
+    const int nb = r >= 4 ? 4 : (int)r;                 // row blocks of A and C (events: 2 + 4 + 2 * 4 <= 16)
+    const int64_t nB = k * c;
+    const int nbB = nB >= 4 ? 4 : 1;                    // chunks of B
+    int ne = 0;
+    auto next_event = [&](cudaStream_t s, cudaEvent_t *out) {
+        *out = ev[ne++];
+        return cudaEventRecord(*out, s) == cudaSuccess ? PMLG_OK : PMLG_ECUDA;
+    };
+    cudaEvent_t e;
+    PMLG_TRY(next_event(st, &e));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(hs, e, 0));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, e, 0));
+    for (int q = 0; q < nbB; q++) {
+        const int64_t f0 = nB * q / nbB, f1 = nB * (q + 1) / nbB;
+        PMLG_TRY(h2d(ctx, dB + f0 * len2, B + f0 * len2, (size_t)((f1 - f0) * len2) * 8, hs));
+        PMLG_TRY(next_event(hs, &e));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
+        PMLG_TRY(product_forward(ctx, j, plan, b, 1, f0, f1, st));
     }
-    PMLG_CUDA_TRY(cudaEventRecord(ev[6], cs));
-    PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ev[6], 0));
+    cudaEvent_t arows[4];
+    for (int i = 0; i < nb; i++) {
+        const int64_t i0 = r * i / nb, i1 = r * (i + 1) / nb;
+        PMLG_TRY(h2d(ctx, dA + i0 * k * len1, A + i0 * k * len1, (size_t)((i1 - i0) * k * len1) * 8, hs));
+        PMLG_TRY(next_event(hs, &arows[i]));
+    }
+    for (int i = 0; i < nb; i++) {
+        const int64_t i0 = r * i / nb, i1 = r * (i + 1) / nb;
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, arows[i], 0));
+        PMLG_TRY(product_forward(ctx, j, plan, b, 0, i0 * k, i1 * k, st));
+        PMLG_TRY(product_pointwise(ctx, j, plan, b, i0, i1, ctx->form, st));
+        PMLG_TRY(product_inverse(ctx, j, plan, b, i0 * c, i1 * c, st));
+        PMLG_TRY(next_event(st, &e));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, e, 0));
+        PMLG_CUDA_TRY(cudaMemcpyAsync(C + i0 * c * clen, dC + i0 * c * clen, (size_t)((i1 - i0) * c * clen) * 8,
+                                      cudaMemcpyDeviceToHost, ds));
+    }
+    PMLG_TRY(next_event(ds, &e));
+    PMLG_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
     return device_status(ctx, st);
 }
 

@@ -235,3 +235,21 @@ def test_batched_uneven(ctx):
     torch.cuda.synchronize()
     for o, ref in zip(outs, refs):
         assert np.array_equal(to_host(o), ref)
+
+
+@pytest.mark.parametrize("dims", [(7, 5, 3, 60, 45), (1, 4, 4, 33, 20), (3, 3, 9, 128, 100), (16, 16, 16, 256, 256)])
+@pytest.mark.parametrize("prime", ["ntt", "p59", "p30"])
+def test_host_path_row_blocks(ctx, dims, prime):
+    """The host-buffer product copies B first and A in row blocks whose rows of C go
+    back while the next rows of A arrive: row counts that do not divide into the
+    blocks, one row, and moduli that take one NTT prime or CRT over several,
+    bit-exact against the oracle and against the device entry point."""
+    import pml_gb300
+    r, k, c, l1, l2 = dims
+    p = {"ntt": P998, "p59": oracle.rand_prime(59, 77), "p30": oracle.rand_prime(30, 78)}[prime]
+    A = oracle.rand_poly_mat(r, k, l1, p, 300 + r)
+    B = oracle.rand_poly_mat(k, c, l2, p, 400 + c)
+    Ch = pml_gb300.nmod_poly_mat_multiply(A, B, p, ctx=ctx)
+    assert np.array_equal(Ch, oracle.poly_mat_mul(A, B, p, nthreads=8))
+    Cd = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), p, ctx=ctx))
+    assert np.array_equal(Ch, Cd)
