@@ -137,7 +137,7 @@ struct pmlg_ctx
     cudaStream_t bstream[kBatchStreams] = {};
     cudaEvent_t bevent[kBatchStreams + 1] = {};
     // events of the host-buffer product's copy/compute pipeline
-    static constexpr int kHostEvents = 16;
+    static constexpr int kHostEvents = 40;
     cudaEvent_t hevent[kHostEvents] = {};
     pmlg::Workspace ws_batch;      // per-stream scratch of the batched products
     // cached NTT tables

@@ -305,6 +305,13 @@ static int check_common(pmlg_ctx *ctx, const void *C, const void *A, const void 
 }
 
 // host -> device copy on the stream (asynchronous when the source is pinned)
+#ifndef PMLG_HOST_ROW_BLOCKS
+#define PMLG_HOST_ROW_BLOCKS 4
+#endif
+// row blocks of the host-buffer product's pipeline (events used: 2 + 4 + 2 * blocks)
+constexpr int kHostRowBlocks = PMLG_HOST_ROW_BLOCKS;
+static_assert(2 + 4 + 2 * kHostRowBlocks <= pmlg_ctx::kHostEvents, "host pipeline events");
+
 static int h2d(pmlg_ctx *ctx, void *dst, const void *src, size_t bytes, cudaStream_t st)
 {
     if (!bytes) return PMLG_OK;
@@ -403,7 +410,7 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
     // its rows of A are in, and copied back while the next rows of A arrive.
     cudaStream_t hs = ctx->bstream[0], ds = ctx->bstream[1];
     cudaEvent_t *ev = ctx->hevent;
-    const int nb = r >= 4 ? 4 : (int)r;                 // row blocks of A and C (events: 2 + 4 + 2 * 4 <= 16)
+    const int nb = r >= kHostRowBlocks ? kHostRowBlocks : (int)r;   // row blocks of A and C
     const int64_t nB = k * c;
     const int nbB = nB >= 4 ? 4 : 1;                    // chunks of B
     int ne = 0;
@@ -422,7 +429,7 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
         PMLG_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
         PMLG_TRY(product_forward(ctx, j, plan, b, 1, f0, f1, st));
     }
-    cudaEvent_t arows[4];
+    cudaEvent_t arows[kHostRowBlocks];
     for (int i = 0; i < nb; i++) {
         const int64_t i0 = r * i / nb, i1 = r * (i + 1) / nb;
         PMLG_TRY(h2d(ctx, dA + i0 * k * len1, A + i0 * k * len1, (size_t)((i1 - i0) * k * len1) * 8, hs));
