@@ -186,6 +186,23 @@ PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_c
                                const uint64_t *F, int64_t m, int64_t n, int64_t flen,
                                int64_t order, uint64_t p, int64_t *appbas_len, void *stream);
 
+/* Left kernel basis of the m x n polynomial matrix pmat (device, entry stride
+ * plen), by the Zhou-Labahn-Storjohann recursion through approximant bases.
+ * shift (host, m entries): in = the shift s; out: the s-row degrees of the
+ * kernel rows in [0, *nullity).  pivind (host, m entries): out, their s-pivot
+ * indices (increasing).  ker: device, m x m of capacity ker_cap; rows
+ * [0, *nullity) receive the basis, in s-ordered weak Popov form, the other rows
+ * are zero.  *ker_len receives the basis' max length (at least 1); when it is
+ * above ker_cap, PMLG_ELEN is returned and nothing is written, so the caller can
+ * retry with a larger buffer.  m <= 64, p a prime < 2^30.  The stream is
+ * synchronised before return.
+ * Replaces nmod_poly_mat_kernel_zls_approx
+ * (flint-extras/src/nmod_poly_mat_extra/kernel.c:232-480), and
+ * nmod_poly_mat_kernel (kernel.c:26-144) with orientation ROW_LOWER. */
+PMLG_API int pmlg_kernel_zls(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
+                             int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
+                             int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* L1: modular dot products and multimodular reduction / CRT               */
 /* ---------------------------------------------------------------------- */

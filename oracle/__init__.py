@@ -60,6 +60,9 @@ def lib():
             "orc_nmod32_vec_mdot": (None, [_u32p, _u32p, _u32p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64]),
             "orc_multimod_reduce": (None, [_u64p, _u64p, C.c_int64, _u64p, C.c_int]),
             "orc_multimod_crt": (None, [_u64p, _u64p, C.c_int64, _u64p, C.c_int, C.c_uint64]),
+            "orc_kernel_zls": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
+                                           C.c_int64, C.c_uint64, C.c_int]),
+            "orc_free": (None, [C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -226,6 +229,48 @@ def is_approximant_basis(appbas: np.ndarray, F: np.ndarray, order: int, shift_in
     _, n, flen = F.shape
     sh = np.ascontiguousarray(shift_in, dtype=np.int64)
     return int(lib().orc_is_approximant_basis(_p64(appbas), alen, _p64(F), flen, m, n, order, _pi64(sh), p))
+
+
+# ---- kernel basis ----------------------------------------------------------
+
+def kernel_zls(pmat: np.ndarray, shift, p: int, nthreads: int = 1):
+    """Left kernel basis by ZLS via approximant bases (kernel.c:232-480).
+    Returns (ker, pivind, rdeg, nullity): ker is the (nullity, m, L) array of the
+    kernel rows, pivind and rdeg their s-pivot indices and s-row degrees."""
+    P = _c64(pmat)
+    m, n, plen = P.shape
+    sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+    piv = np.zeros(max(m, 1), dtype=np.int64)
+    kp = _u64p()
+    L = C.c_int64(0)
+    nul = int(lib().orc_kernel_zls(C.byref(kp), C.byref(L), _pi64(piv), _pi64(sh), _p64(P), m, n, plen, p,
+                                   nthreads))
+    flat = np.ctypeslib.as_array(kp, shape=(m * m * L.value,)).copy() if m else np.zeros(0, dtype=np.uint64)
+    lib().orc_free(C.cast(kp, C.c_void_p))
+    ker = flat.reshape(m, m, L.value)[:nul] if m else np.zeros((0, 0, 1), dtype=np.uint64)
+    return ker, piv[:nul].copy(), sh[:nul].copy(), nul
+
+
+def row_degrees_and_pivots(ker: np.ndarray, shift):
+    """s-row degrees and s-pivot indices (the rightmost column reaching the
+    s-row degree: ROW_LOWER) of the rows of a polynomial matrix."""
+    rows, cols, L = ker.shape
+    deg = np.full((rows, cols), -1, dtype=np.int64)
+    nz = ker != 0
+    for d in range(L):
+        deg[nz[:, :, d]] = d
+    rdeg, piv = [], []
+    for i in range(rows):
+        best, bj = None, -1
+        for j in range(cols):
+            if deg[i, j] < 0:
+                continue
+            v = int(deg[i, j]) + int(shift[j])
+            if best is None or v >= best:
+                best, bj = v, j
+        rdeg.append(best if best is not None else None)
+        piv.append(bj)
+    return rdeg, piv
 
 
 # ---- dot products, CRT ------------------------------------------------------

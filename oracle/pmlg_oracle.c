@@ -1146,3 +1146,328 @@ void orc_multimod_crt(uint64_t *out, const uint64_t *residues, int64_t nb,
         out[i] = x;
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* kernel basis, Zhou-Labahn-Storjohann via approximant bases          */
+/* (nmod_poly_mat_kernel_zls_approx, kernel.c:232-480)                 */
+/* ------------------------------------------------------------------ */
+
+/* a polynomial matrix: entry (i, j) at a + (i * c + j) * cap */
+typedef struct
+{
+    uint64_t *a;
+    int64_t r, c, cap;
+} kpm_t;
+
+static kpm_t kpm_zero(int64_t r, int64_t c, int64_t cap)
+{
+    kpm_t P;
+    P.r = r; P.c = c; P.cap = cap > 0 ? cap : 1;
+    P.a = (uint64_t *) calloc((size_t) (r * c * P.cap + 1), sizeof(uint64_t));
+    return P;
+}
+
+static void kpm_free(kpm_t *P)
+{
+    free(P->a);
+    P->a = NULL;
+}
+
+static kpm_t kpm_identity(int64_t m)
+{
+    kpm_t P = kpm_zero(m, m, 1);
+    for (int64_t i = 0; i < m; i++)
+        P.a[(i * m + i) * P.cap] = 1;
+    return P;
+}
+
+static int64_t kpm_len(const kpm_t *P)
+{
+    return orc_pm_max_length(P->a, P->r, P->c, P->cap);
+}
+
+/* rows [r0, r1) and columns [c0, c1), capacity kept */
+static kpm_t kpm_window(const kpm_t *P, int64_t r0, int64_t r1, int64_t c0, int64_t c1)
+{
+    kpm_t Q = kpm_zero(r1 - r0, c1 - c0, P->cap);
+    for (int64_t i = r0; i < r1; i++)
+        for (int64_t j = c0; j < c1; j++)
+            memcpy(Q.a + ((i - r0) * Q.c + (j - c0)) * Q.cap, P->a + (i * P->c + j) * P->cap,
+                   sizeof(uint64_t) * (size_t) P->cap);
+    return Q;
+}
+
+/* A * B (nmod_poly_mat_multiply) */
+static kpm_t kpm_mul(const kpm_t *A, const kpm_t *B, uint64_t p, int nthreads)
+{
+    const int64_t la = kpm_len(A), lb = kpm_len(B);
+    if (la == 0 || lb == 0)
+        return kpm_zero(A->r, B->c, 1);
+    uint64_t *At = pm_recap(A->a, A->r, A->c, A->cap, la);
+    uint64_t *Bt = pm_recap(B->a, B->r, B->c, B->cap, lb);
+    kpm_t C = kpm_zero(A->r, B->c, la + lb - 1);
+    pm_mul_auto(C.a, At, Bt, A->r, A->c, B->c, la, lb, p, nthreads);
+    free(At); free(Bt);
+    return C;
+}
+
+/* rows[i] <- rows[perm[i]] for i < nrows, and store[i] <- store[perm[i]]
+ * (nmod_poly_mat_permute_rows, nmod_poly_mat_utils.h:264) */
+static void kpm_permute_rows(kpm_t *P, int64_t nrows, const int64_t *perm, int64_t *store)
+{
+    const size_t row = (size_t) (P->c * P->cap);
+    uint64_t *tmp = (uint64_t *) malloc(sizeof(uint64_t) * row * (size_t) (nrows > 0 ? nrows : 1));
+    for (int64_t i = 0; i < nrows; i++)
+        memcpy(tmp + (size_t) i * row, P->a + (size_t) perm[i] * row, sizeof(uint64_t) * row);
+    memcpy(P->a, tmp, sizeof(uint64_t) * row * (size_t) nrows);
+    free(tmp);
+    if (store)
+    {
+        int64_t *t = (int64_t *) malloc(sizeof(int64_t) * (size_t) (nrows > 0 ? nrows : 1));
+        for (int64_t i = 0; i < nrows; i++)
+            t[i] = store[perm[i]];
+        memcpy(store, t, sizeof(int64_t) * (size_t) nrows);
+        free(t);
+    }
+}
+
+/* rows [0, k) of P replaced by the rows of Q (same column count), capacity grown as needed */
+static void kpm_set_rows(kpm_t *P, const kpm_t *Q, int64_t k)
+{
+    if (Q->cap > P->cap)
+    {
+        uint64_t *a = pm_recap(P->a, P->r, P->c, P->cap, Q->cap);
+        free(P->a);
+        P->a = a;
+        P->cap = Q->cap;
+    }
+    for (int64_t i = 0; i < k; i++)
+        for (int64_t j = 0; j < P->c; j++)
+        {
+            uint64_t *d = P->a + (i * P->c + j) * P->cap;
+            memset(d, 0, sizeof(uint64_t) * (size_t) P->cap);
+            memcpy(d, Q->a + (i * Q->c + j) * Q->cap, sizeof(uint64_t) * (size_t) Q->cap);
+        }
+}
+
+static int64_t kzls(kpm_t *ker, int64_t *pivind, int64_t *shift, const kpm_t *pm, uint64_t p, int nt)
+{
+    const int64_t m = pm->r, n = pm->c;
+    /* empty matrices, or single row/column vectors that are zero (:240-248) */
+    if (m == 0 || n == 0 || ((m == 1 || n == 1) && kpm_len(pm) == 0))
+    {
+        *ker = kpm_identity(m);
+        for (int64_t i = 0; i < m; i++)
+            pivind[i] = i;
+        return m;
+    }
+    /* one nonzero row (:251-252) */
+    if (m == 1)
+    {
+        *ker = kpm_zero(m, m, 1);
+        return 0;
+    }
+    /* 2n > m: split the columns [n - n/2 | n/2] (:256-317) */
+    if (2 * n > m)
+    {
+        const int64_t n1 = n - n / 2;
+        kpm_t left = kpm_window(pm, 0, m, 0, n1);
+        kpm_t k1;
+        int64_t nullity = kzls(&k1, pivind, shift, &left, p, nt);
+        kpm_free(&left);
+        if (nullity == 0)
+        {
+            *ker = k1;
+            return 0;
+        }
+        kpm_t ker1 = kpm_window(&k1, 0, nullity, 0, m);
+        kpm_t right = kpm_window(pm, 0, m, n1, n);
+        kpm_t resid = kpm_mul(&ker1, &right, p, nt);
+        kpm_free(&right);
+        kpm_t k2;
+        int64_t *piv2 = (int64_t *) malloc(sizeof(int64_t) * (size_t) nullity);
+        const int64_t nullity2 = kzls(&k2, piv2, shift, &resid, p, nt);
+        kpm_free(&resid);
+        if (nullity2 > 0)
+        {
+            kpm_t k2top = kpm_window(&k2, 0, nullity2, 0, nullity);
+            kpm_t k3 = kpm_mul(&k2top, &ker1, p, nt);
+            kpm_set_rows(&k1, &k3, nullity2);
+            for (int64_t i = 0; i < nullity2; i++)
+                pivind[i] = pivind[piv2[i]];
+            kpm_free(&k2top);
+            kpm_free(&k3);
+        }
+        kpm_free(&k2);
+        kpm_free(&ker1);
+        free(piv2);
+        *ker = k1;
+        return nullity2;
+    }
+
+    /* 1 <= n <= m/2 (:321-479) */
+    int64_t *buf = (int64_t *) malloc(sizeof(int64_t) * (size_t) m);
+    int64_t nnz = 0;
+    for (int64_t i = 0; i < m; i++)
+    {
+        int64_t mx = -1;
+        for (int64_t j = 0; j < n; j++)
+        {
+            const int64_t d = poly_deg(pm->a + (i * n + j) * pm->cap, pm->cap);
+            if (d > mx) mx = d;
+        }
+        if (mx >= 0) { nnz++; buf[i] = mx; }
+        else buf[i] = 0;
+    }
+    if (nnz == 0)
+    {
+        *ker = kpm_identity(m);
+        for (int64_t i = 0; i < m; i++)
+            pivind[i] = i;
+        free(buf);
+        return m;
+    }
+    int64_t maxdeg = buf[0], diff_shift = shift[0] - buf[0];
+    for (int64_t i = 1; i < m; i++)
+    {
+        if (buf[i] > maxdeg) maxdeg = buf[i];
+        if (diff_shift > shift[i] - buf[i]) diff_shift = shift[i] - buf[i];
+    }
+    /* order = 1 + max(maxdeg, 1 + floor((sum(shift) - m * diff_shift - 1) / (m - n)))
+     * with C's truncating division, as the reference computes it (:352-356) */
+    int64_t order = -m * diff_shift - 1;
+    for (int64_t i = 0; i < m; i++)
+        order += shift[i];
+    order = 1 + order / (m - n);
+    order = 1 + (maxdeg > order ? maxdeg : order);
+
+    const int64_t plen = kpm_len(pm) > 0 ? kpm_len(pm) : 1;
+    uint64_t *pmt = pm_recap(pm->a, m, n, pm->cap, plen);
+    kpm_t K = kpm_zero(m, m, order + 1);
+    orc_pmbasis(K.a, shift, pmt, m, n, plen, order, p, 32, nt);
+
+    /* rows of the approximant basis that are kernel rows (:361-382) */
+    int64_t nullity = 0, sum_pmatdeg = 0;
+    int no_constant_pivot_and_row = 1;
+    for (int64_t i = 0; i < m; i++)
+    {
+        if (shift[i] < order + diff_shift)
+            pivind[nullity++] = i;
+        else
+        {
+            if (buf[i] == 0 && poly_deg(K.a + (i * m + i) * K.cap, K.cap) <= 0)
+                no_constant_pivot_and_row = 0;
+            sum_pmatdeg += buf[i];
+            buf[i - nullity] = i;
+        }
+    }
+    for (int64_t i = nullity; i < m; i++)
+        pivind[i] = buf[i - nullity];
+    kpm_permute_rows(&K, m, pivind, shift);
+
+    /* early exit (:392-404) */
+    if (nullity >= m - n && no_constant_pivot_and_row)
+    {
+        int64_t sum_pivdeg = 0;
+        for (int64_t i = 0; i < nullity; i++)
+            sum_pivdeg += poly_deg(K.a + (i * m + pivind[i]) * K.cap, K.cap);
+        if (sum_pivdeg == sum_pmatdeg)
+        {
+            free(buf); free(pmt);
+            *ker = K;
+            return nullity;
+        }
+    }
+
+    /* residual of the other rows, its kernel, and the missing kernel rows (:406-441) */
+    kpm_t approx = kpm_window(&K, nullity, m, 0, m);
+    kpm_t resid = kpm_zero(m - nullity, n, maxdeg + 1);
+    {
+        const int64_t la = kpm_len(&approx) > 0 ? kpm_len(&approx) : 1;
+        uint64_t *At = pm_recap(approx.a, m - nullity, m, approx.cap, la);
+        orc_poly_mat_mulmid(resid.a, At, pmt, m - nullity, m, n, la, plen, order, order + maxdeg + 1, p, nt);
+        free(At);
+    }
+    kpm_t k2;
+    const int64_t nullity2 = kzls(&k2, buf, shift + nullity, &resid, p, nt);
+    kpm_free(&resid);
+    if (nullity2 == 0)
+    {
+        kpm_free(&k2); kpm_free(&approx); free(buf); free(pmt);
+        *ker = K;
+        return nullity;
+    }
+    {
+        kpm_t k2top = kpm_window(&k2, 0, nullity2, 0, m - nullity);
+        kpm_t prod = kpm_mul(&k2top, &approx, p, nt);
+        /* rows [nullity, nullity + nullity2) of K <- prod */
+        kpm_t tail = kpm_window(&K, nullity, m, 0, m);
+        kpm_set_rows(&tail, &prod, nullity2);
+        if (tail.cap > K.cap)
+        {
+            uint64_t *a = pm_recap(K.a, m, m, K.cap, tail.cap);
+            free(K.a);
+            K.a = a;
+            K.cap = tail.cap;
+        }
+        for (int64_t i = 0; i < m - nullity; i++)
+            for (int64_t j = 0; j < m; j++)
+            {
+                uint64_t *d = K.a + ((nullity + i) * m + j) * K.cap;
+                memset(d, 0, sizeof(uint64_t) * (size_t) K.cap);
+                memcpy(d, tail.a + (i * m + j) * tail.cap, sizeof(uint64_t) * (size_t) tail.cap);
+            }
+        kpm_free(&k2top); kpm_free(&prod); kpm_free(&tail);
+    }
+    for (int64_t i = 0; i < nullity2; i++)
+        pivind[nullity + i] = pivind[nullity + buf[i]];
+
+    /* merge the two sorted pivot lists, permuting rows, pivots and shifts (:443-468) */
+    const int64_t tot = nullity + nullity2;
+    int64_t i1 = 0, i2 = 0;
+    for (int64_t i = 0; i < tot; i++)
+    {
+        if (i2 == nullity2 || (i1 < nullity && pivind[i1] < pivind[nullity + i2]))
+            buf[i] = i1++;
+        else
+            buf[i] = nullity + i2++;
+    }
+    kpm_permute_rows(&K, tot, buf, NULL);
+    int64_t *t = (int64_t *) malloc(sizeof(int64_t) * (size_t) tot);
+    for (int64_t i = 0; i < tot; i++) t[i] = pivind[i];
+    for (int64_t i = 0; i < tot; i++) pivind[i] = t[buf[i]];
+    for (int64_t i = 0; i < tot; i++) t[i] = shift[i];
+    for (int64_t i = 0; i < tot; i++) shift[i] = t[buf[i]];
+    free(t);
+    kpm_free(&k2); kpm_free(&approx); free(buf); free(pmt);
+    *ker = K;
+    return tot;
+}
+
+int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift,
+                       const uint64_t *pmat, int64_t m, int64_t n, int64_t plen, uint64_t p,
+                       int nthreads)
+{
+    kpm_t P;
+    P.r = m; P.c = n; P.cap = plen > 0 ? plen : 1;
+    P.a = pm_recap(pmat, m, n, plen > 0 ? plen : 0, P.cap);
+    kpm_t K;
+    const int64_t nullity = kzls(&K, pivind, shift, &P, p, nthreads);
+    kpm_free(&P);
+    /* the kernel rows, capacity their max length (at least 1); other rows zero */
+    kpm_t rows = kpm_window(&K, 0, nullity, 0, m);
+    const int64_t L = kpm_len(&rows) > 0 ? kpm_len(&rows) : 1;
+    uint64_t *out = (uint64_t *) calloc((size_t) (m * m * L + 1), sizeof(uint64_t));
+    for (int64_t e = 0; e < nullity * m; e++)
+        memcpy(out + e * L, rows.a + e * rows.cap, sizeof(uint64_t) * (size_t) (L < rows.cap ? L : rows.cap));
+    kpm_free(&rows);
+    kpm_free(&K);
+    *ker = out;
+    *klen = L;
+    return nullity;
+}
+
+void orc_free(void *ptr)
+{
+    free(ptr);
+}

@@ -137,6 +137,19 @@ void orc_multimod_reduce(uint64_t *residues, const uint64_t *input, int64_t nb,
 void orc_multimod_crt(uint64_t *out, const uint64_t *residues, int64_t nb,
                       const uint64_t *primes, int nprimes, uint64_t p);
 
+/* ---- kernel basis (flint-extras/src/nmod_poly_mat_extra/kernel.c) ---- */
+/* nmod_poly_mat_kernel_zls_approx (kernel.c:232-480), left kernel (ROW_LOWER) of
+ * the m x n matrix pmat (entry capacity plen).  shift: m entries, in = s, out: the
+ * s-row degrees of the kernel rows in [0, nullity); pivind: m entries, out: the
+ * s-pivot indices of the kernel rows in [0, nullity).  *ker receives an m x m
+ * matrix (free it with orc_free) of capacity *klen whose rows [0, nullity) are the
+ * kernel basis, in s-ordered weak Popov form with increasing pivots; its other
+ * rows are zero.  Returns the nullity. */
+int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift,
+                       const uint64_t *pmat, int64_t m, int64_t n, int64_t plen, uint64_t p,
+                       int nthreads);
+void orc_free(void *ptr);
+
 #ifdef __cplusplus
 }
 #endif

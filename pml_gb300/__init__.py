@@ -29,7 +29,7 @@ from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_F16_TC, FORM_INT8_TC, PmlgErro
 __all__ = [
     "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
-    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_vec_dot_product", "nmod32_vec_dot_product",
+    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_kernel", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
 ]
 
@@ -256,6 +256,36 @@ def nmod_poly_mat_mbasis(F, order: int, shift, p: int, ctx: Optional[Context] = 
     """nmod_poly_mat_mbasis (approximant_basis.c:18), CUDA tensors only."""
     ctx = _ctx(ctx, F)
     return _approx(ctx.lib.pmlg_mbasis, None, F, order, shift, p, ctx)
+
+
+# ---------------------------------------------------------------------------
+# L5: kernel bases
+# ---------------------------------------------------------------------------
+
+def nmod_poly_mat_kernel(pmat, shift, p: int, ctx: Optional[Context] = None, cap: Optional[int] = None):
+    """Left kernel basis (ROW_LOWER) of the (m, n, len) CUDA tensor pmat:
+    nmod_poly_mat_kernel_zls_approx (kernel.c:232).  Returns (ker, pivind, rdeg):
+    ker has shape (nullity, m, length), in shift-ordered weak Popov form; pivind
+    and rdeg are its shift-pivot indices and shift-row degrees."""
+    import torch
+    _require_cuda(pmat)
+    ctx = _ctx(ctx, pmat)
+    m, n, plen = pmat.shape
+    cap = cap or max(1, (min(m, n) + 1) * max(plen, 1) + 1)
+    while True:
+        sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+        piv = np.zeros(max(m, 1), dtype=np.int64)
+        ker = torch.zeros((m, m, cap), dtype=torch.int64, device=pmat.device)
+        ln, nul = C.c_int64(0), C.c_int64(0)
+        st = ctx.lib.pmlg_kernel_zls(ctx.handle, _ptr(ker), cap, C.byref(ln), piv.ctypes.data_as(C.POINTER(C.c_int64)),
+                                     sh.ctypes.data_as(C.POINTER(C.c_int64)), _ptr(pmat), m, n, plen, p,
+                                     C.byref(nul), _stream_ptr(pmat))
+        if st == 4 and ln.value > cap:   # PMLG_ELEN: the basis is longer than the buffer
+            cap = int(ln.value)
+            continue
+        ctx.check(st)
+        k = int(nul.value)
+        return ker[:k, :, :max(int(ln.value), 1)], piv[:k].copy(), sh[:k].copy()
 
 
 # ---------------------------------------------------------------------------

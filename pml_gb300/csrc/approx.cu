@@ -1039,6 +1039,14 @@ static int approx_entry(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *s
     return PMLG_OK;
 }
 
+int pmbasis_device(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *shift, const uint64_t *F,
+                   int64_t m, int64_t n, int64_t flen, int64_t order, uint64_t p, int64_t *len,
+                   cudaStream_t st)
+{
+    const int64_t leaf = ctx->leaf_order > 0 ? ctx->leaf_order : 32;
+    return approx_entry(ctx, appbas, cap, shift, F, m, n, flen, order, p, len, st, leaf);
+}
+
 }  // namespace pmlg
 
 using namespace pmlg;

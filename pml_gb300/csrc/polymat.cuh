@@ -37,4 +37,17 @@ int mulmid_prepare(ProductJob &j, int64_t len1, int64_t len2, int64_t nlo, int64
 
 int lg_for(int64_t n);
 
+// Dense device products (entry strides len1, len2; C: len1 + len2 - 1, res: nhi - nlo).
+int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B, int64_t r,
+                        int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p, cudaStream_t st);
+int poly_mat_mulmid_device(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, const uint64_t *B,
+                           int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2, int64_t nlo,
+                           int64_t nhi, uint64_t p, cudaStream_t st);
+
+// pmbasis on device buffers (appbas capacity cap >= order + 1, F entry stride flen),
+// shift on the host; *len is appbas' exact max length.
+int pmbasis_device(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *shift, const uint64_t *F,
+                   int64_t m, int64_t n, int64_t flen, int64_t order, uint64_t p, int64_t *len,
+                   cudaStream_t st);
+
 }  // namespace pmlg

@@ -1,0 +1,67 @@
+"""GPU parity of the left kernel basis (pmlg_kernel_zls through pml_gb300):
+the basis, its pivot indices and shifted row degrees equal the oracle's
+(kernel.c:232-480 restated) bit for bit, on the shapes and shift families of
+the reference's t-kernel.c, with its degenerate inputs (zero matrix, zero
+rows, dependent columns, a single row or column)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import P998, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_kernel(ctx, F, shift, p, cap=None):
+    import pml_gb300
+    ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel(to_dev(F), shift, p, ctx=ctx, cap=cap)
+    return to_host(ker), list(piv), list(rdeg)
+
+
+def _same(ctx, F, shift, p):
+    ker, piv, rdeg = _gpu_kernel(ctx, F, shift, p)
+    rker, rpiv, rrdeg, nul = oracle.kernel_zls(F, shift, p, nthreads=8)
+    assert ker.shape[0] == nul
+    assert piv == list(rpiv) and rdeg == list(rrdeg)
+    L = max(ker.shape[2], rker.shape[2])
+    pad = lambda a: np.concatenate([a, np.zeros(a.shape[:2] + (L - a.shape[2],), dtype=np.uint64)], axis=2)
+    assert np.array_equal(pad(ker), pad(rker))
+    return ker, piv, rdeg
+
+
+@pytest.mark.parametrize("dims", [(4, 2, 3), (8, 3, 4), (10, 4, 6), (5, 3, 4), (16, 4, 8), (20, 7, 5),
+                                  (7, 6, 3), (9, 9, 2), (2, 5, 3), (32, 12, 10), (48, 16, 6), (64, 20, 4)])
+def test_kernel_random(ctx, dims):
+    m, n, d = dims
+    p = P998
+    F = oracle.rand_poly_mat(m, n, d + 1, p, 100 + m + n)
+    for shift in ([0] * m, list(range(m)), [(7 * i) % 5 for i in range(m)]):
+        _same(ctx, F, shift, p)
+
+
+def test_kernel_degenerate(ctx):
+    p = P998
+    m = 6
+    ker, piv, rdeg = _same(ctx, np.zeros((m, 3, 4), dtype=np.uint64), [0] * m, p)
+    assert len(piv) == m
+    F = oracle.rand_poly_mat(m, 3, 5, p, 9)
+    F[2] = 0
+    F[:, 2] = F[:, 0]
+    _same(ctx, F, [0] * m, p)
+    _same(ctx, oracle.rand_poly_mat(1, 3, 4, p, 10), [0], p)
+    _same(ctx, oracle.rand_poly_mat(5, 1, 4, p, 11), [0] * 5, p)
+    _same(ctx, oracle.rand_poly_mat(12, 4, 6, 536870923, 12), [0] * 12, 536870923)
+
+
+def test_kernel_property_and_small_buffer(ctx):
+    """K * F = 0 through the GPU product, and a buffer shorter than the basis is
+    reported (PMLG_ELEN with the needed length) and then filled on retry."""
+    import pml_gb300
+    p = P998
+    F = oracle.rand_poly_mat(24, 8, 9, p, 31)
+    ker, piv, rdeg = _gpu_kernel(ctx, F, [0] * 24, p, cap=1)
+    assert ker.shape[0] == 16
+    prod = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(ker), to_dev(F), p, ctx=ctx))
+    assert not prod.any()
