@@ -359,6 +359,29 @@ def measure_batched_uneven(ctx, dev, st, forms, rank):
     return res
 
 
+def measure_kernel_basis(ctx, dev, st, rank):
+    """Left kernel basis of a 64x32 polynomial matrix of degree 1023, zero shift
+    (nmod_poly_mat_kernel_zls_approx, kernel.c:232; the shape of the reference's
+    p-kernel.c profiler): wall clock around one call (it synchronises internally)
+    after one warm-up call, and K * F = 0 checked with the GPU product."""
+    import time
+    import torch
+    import pml_gb300
+    m, n, ln = 64, 32, 1024
+    rng = np.random.default_rng(21 + rank)
+    F = torch.from_numpy(rng.integers(0, P, size=(m, n, ln), dtype=np.uint64).view(np.int64)).to(dev)
+    pml_gb300.nmod_poly_mat_kernel(F, [0] * m, P, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel(F, [0] * m, P, ctx=ctx)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    zero = not bool(pml_gb300.nmod_poly_mat_multiply(ker, F, P, ctx=ctx).any().item())
+    return {"ms": ms, "nullity": int(ker.shape[0]), "basis_length": int(ker.shape[2]), "kernel_times_F_zero": zero,
+            "config": "kernel basis of a 64x32 matrix, degree 1023, zero shift, p = 998244353, uniform coefficients",
+            "timing": "wall clock around one call after one warm-up call"}
+
+
 def run_pml(args):
     import torch
     rank, world, local = dist_env()
@@ -537,6 +560,7 @@ def run_pml(args):
     extra = {} if args.no_extra else {
         "pointwise_batch": measure_pointwise_batch(ctx, dev, st, FORMS, rank),
         "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
+        "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
     }
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)

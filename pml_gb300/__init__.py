@@ -285,7 +285,7 @@ def nmod_poly_mat_kernel(pmat, shift, p: int, ctx: Optional[Context] = None, cap
             continue
         ctx.check(st)
         k = int(nul.value)
-        return ker[:k, :, :max(int(ln.value), 1)], piv[:k].copy(), sh[:k].copy()
+        return ker[:k, :, :max(int(ln.value), 1)].contiguous(), piv[:k].copy(), sh[:k].copy()
 
 
 # ---------------------------------------------------------------------------
