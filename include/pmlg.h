@@ -202,6 +202,10 @@ PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_c
 PMLG_API int pmlg_kernel_zls(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
                              int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
                              int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
+/* Host-buffer form of pmlg_kernel_zls (ker and pmat in host memory). */
+PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
+                                  int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
+                                  int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
 
 /* ---------------------------------------------------------------------- */
 /* L1: modular dot products and multimodular reduction / CRT               */

@@ -263,29 +263,39 @@ def nmod_poly_mat_mbasis(F, order: int, shift, p: int, ctx: Optional[Context] = 
 # ---------------------------------------------------------------------------
 
 def nmod_poly_mat_kernel(pmat, shift, p: int, ctx: Optional[Context] = None, cap: Optional[int] = None):
-    """Left kernel basis (ROW_LOWER) of the (m, n, len) CUDA tensor pmat:
+    """Left kernel basis (ROW_LOWER) of the (m, n, len) matrix pmat (a CUDA tensor,
+    or a numpy array through the host-buffer entry point):
     nmod_poly_mat_kernel_zls_approx (kernel.c:232).  Returns (ker, pivind, rdeg):
     ker has shape (nullity, m, length), in shift-ordered weak Popov form; pivind
     and rdeg are its shift-pivot indices and shift-row degrees."""
-    import torch
-    _require_cuda(pmat)
     ctx = _ctx(ctx, pmat)
+    dev = _is_torch(pmat)
+    if dev:
+        import torch
+        _require_cuda(pmat)
+    else:
+        pmat = np.ascontiguousarray(pmat, dtype=np.uint64)
     m, n, plen = pmat.shape
     cap = cap or max(1, (min(m, n) + 1) * max(plen, 1) + 1)
     while True:
         sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
         piv = np.zeros(max(m, 1), dtype=np.int64)
-        ker = torch.zeros((m, m, cap), dtype=torch.int64, device=pmat.device)
+        if dev:
+            ker = torch.zeros((m, m, cap), dtype=torch.int64, device=pmat.device)
+        else:
+            ker = np.zeros((m, m, cap), dtype=np.uint64)
         ln, nul = C.c_int64(0), C.c_int64(0)
-        st = ctx.lib.pmlg_kernel_zls(ctx.handle, _ptr(ker), cap, C.byref(ln), piv.ctypes.data_as(C.POINTER(C.c_int64)),
-                                     sh.ctypes.data_as(C.POINTER(C.c_int64)), _ptr(pmat), m, n, plen, p,
-                                     C.byref(nul), _stream_ptr(pmat))
+        fn = ctx.lib.pmlg_kernel_zls if dev else ctx.lib.pmlg_kernel_zls_host
+        st = fn(ctx.handle, _ptr(ker), cap, C.byref(ln), piv.ctypes.data_as(C.POINTER(C.c_int64)),
+                sh.ctypes.data_as(C.POINTER(C.c_int64)), _ptr(pmat), m, n, plen, p, C.byref(nul),
+                _stream_ptr(pmat) if dev else None)
         if st == 4 and ln.value > cap:   # PMLG_ELEN: the basis is longer than the buffer
             cap = int(ln.value)
             continue
         ctx.check(st)
         k = int(nul.value)
-        return ker[:k, :, :max(int(ln.value), 1)].contiguous(), piv[:k].copy(), sh[:k].copy()
+        out = ker[:k, :, :max(int(ln.value), 1)]
+        return (out.contiguous() if dev else out.copy()), piv[:k].copy(), sh[:k].copy()
 
 
 # ---------------------------------------------------------------------------

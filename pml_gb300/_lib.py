@@ -47,6 +47,8 @@ SIGNATURES = {
     "pmlg_mbasis": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_pmbasis_host": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_kernel_zls": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p, _vp]),
+    "pmlg_kernel_zls_host": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p,
+                                       _vp]),
     "pmlg_nmod_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
     "pmlg_nmod32_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
     "pmlg_nmod32_vec_mdot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _u64, _vp]),

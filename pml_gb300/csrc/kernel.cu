@@ -437,3 +437,27 @@ extern "C" PMLG_API int pmlg_kernel_zls(pmlg_ctx *ctx, uint64_t *ker, int64_t ke
     if (s == PMLG_OK && cudaStreamSynchronize(st) != cudaSuccess) s = PMLG_ECUDA;
     return s;
 }
+
+extern "C" PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
+                                             int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
+                                             int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream)
+{
+    if (!ctx || m < 0 || n < 0 || plen < 0 || ker_cap < 1) return PMLG_EINVAL;
+    if (m > 0 && !ker) return PMLG_EINVAL;
+    if (m > 0 && n > 0 && plen > 0 && !pmat) return PMLG_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    const size_t bP = (size_t)(m * n * plen) * 8, bK = (size_t)(m * m * ker_cap) * 8;
+    uint64_t *dP = nullptr, *dK = nullptr;
+    PMLG_CUDA_TRY(cudaMallocAsync((void **)&dP, bP + 8, st));
+    cudaError_t e = cudaMallocAsync((void **)&dK, bK + 8, st);
+    int s = e == cudaSuccess ? PMLG_OK : PMLG_ECUDA;
+    if (s == PMLG_OK && bP && cudaMemcpyAsync(dP, pmat, bP, cudaMemcpyHostToDevice, st) != cudaSuccess) s = PMLG_ECUDA;
+    if (s == PMLG_OK) s = pmlg_kernel_zls(ctx, dK, ker_cap, ker_len, pivind, shift, dP, m, n, plen, p, nullity, stream);
+    if (s == PMLG_OK && bK && cudaMemcpyAsync(ker, dK, bK, cudaMemcpyDeviceToHost, st) != cudaSuccess) s = PMLG_ECUDA;
+    if (dK) cudaFreeAsync(dK, st);
+    cudaFreeAsync(dP, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == PMLG_OK) s = PMLG_ECUDA;
+    if (s == PMLG_ECUDA) set_error(ctx, "host-buffer kernel basis: a copy or an allocation failed");
+    return s;
+}

@@ -65,3 +65,13 @@ def test_kernel_property_and_small_buffer(ctx):
     assert ker.shape[0] == 16
     prod = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(ker), to_dev(F), p, ctx=ctx))
     assert not prod.any()
+
+
+def test_kernel_host_path(ctx):
+    """The host-buffer entry point (numpy in, numpy out) equals the device one."""
+    import pml_gb300
+    p = P998
+    F = oracle.rand_poly_mat(10, 4, 7, p, 41)
+    kh, ph, rh = pml_gb300.nmod_poly_mat_kernel(F, list(range(10)), p, ctx=ctx)
+    kd, pd, rd = _gpu_kernel(ctx, F, list(range(10)), p)
+    assert np.array_equal(kh, kd) and list(ph) == pd and list(rh) == rd
