@@ -382,6 +382,37 @@ def measure_kernel_basis(ctx, dev, st, rank):
             "timing": "wall clock around one call after one warm-up call"}
 
 
+def measure_layout(ctx, dev, st, rank, peak_gbs):
+    """Entry-major -> coefficient-major and back for a 64x64 matrix of length 4096
+    (nmod_mat_poly_set_trunc_from_poly_mat / nmod_poly_mat_set_trunc_from_mat_poly):
+    CUDA events around 10 calls each, 16 bytes of traffic per coefficient (inputs of
+    134 MB, larger than L2, so no flush is needed)."""
+    import torch
+    import pml_gb300
+    r = c = 64
+    ln = 4096
+    rng = np.random.default_rng(31 + rank)
+    Pm = torch.from_numpy(rng.integers(0, P, size=(r, c, ln), dtype=np.uint64).view(np.int64)).to(dev)
+    M = torch.empty((ln, r, c), dtype=torch.int64, device=dev)
+    Q = torch.empty((r, c, ln), dtype=torch.int64, device=dev)
+    fwd = lambda: pml_gb300.nmod_mat_poly_set_trunc_from_poly_mat(Pm, ln, ctx=ctx, out=M)
+    # the forward call reads the length back (a synchronisation), so time it without
+    fwd_nolen = lambda: ctx.check(ctx.lib.pmlg_poly_mat_to_mat_poly(ctx.handle, M.data_ptr(), ln, Pm.data_ptr(), r,
+                                                                     c, ln, ln, ln, None, st.cuda_stream))
+    bwd = lambda: pml_gb300.nmod_poly_mat_set_trunc_from_mat_poly(M, ln, ctx=ctx, out=Q)
+    fwd()
+    t_f, _ = _time_calls(fwd_nolen, st, 10, 3)
+    t_b, _ = _time_calls(bwd, st, 10, 3)
+    ok = bool(torch.equal(Pm, Q))
+    nbytes = 2 * r * c * ln * 8
+    res = {"to_mat_poly_ms": t_f, "to_poly_mat_ms": t_b, "round_trip_exact": ok,
+           "to_mat_poly_gbs": nbytes / t_f / 1e6, "to_poly_mat_gbs": nbytes / t_b / 1e6,
+           "config": "64x64 polynomial matrix, length 4096, uint64 coefficients (134 MB each way)"}
+    if peak_gbs:
+        res["frac_of_measured_hbm"] = max(res["to_mat_poly_gbs"], res["to_poly_mat_gbs"]) / peak_gbs
+    return res
+
+
 def run_pml(args):
     import torch
     rank, world, local = dist_env()
@@ -561,6 +592,7 @@ def run_pml(args):
         "pointwise_batch": measure_pointwise_batch(ctx, dev, st, FORMS, rank),
         "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
         "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
+        "layout_conversion": measure_layout(ctx, dev, st, rank, peaks.get("hbm_gbs")),
     }
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)

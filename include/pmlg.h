@@ -207,6 +207,25 @@ PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap,
                                   int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
                                   int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
 
+/* Layout conversions (device buffers).  Entry-major (nmod_poly_mat): entry (i, j)
+ * holds coefficients at [(i*c + j)*ld, (i*c + j)*ld + len).  Coefficient-major
+ * (nmod_mat_poly): coefficient k is the r x c matrix at [k*r*c, (k+1)*r*c).
+ * pmlg_poly_mat_to_mat_poly: out (out_cap >= min(order, len) coefficient
+ * matrices) receives the coefficients k < min(order, len), zeros past them;
+ * *out_len (may be NULL, then nothing synchronises) receives the normalised
+ * length, the last nonzero coefficient matrix + 1.  Replaces
+ * nmod_mat_poly_set_trunc_from_poly_mat
+ * (flint-extras/src/nmod_mat_poly_extra/nmod_mat_poly_set_from.c:31-52).
+ * pmlg_mat_poly_to_poly_mat: out (entries of capacity out_cap >= min(order,
+ * len)) receives the coefficients k < min(order, len), zeros past them.
+ * Replaces nmod_poly_mat_set_trunc_from_mat_poly
+ * (flint-extras/src/nmod_poly_mat_extra/nmod_poly_mat_utils.c:185-210). */
+PMLG_API int pmlg_poly_mat_to_mat_poly(pmlg_ctx *ctx, uint64_t *out, int64_t out_cap, const uint64_t *in,
+                                       int64_t r, int64_t c, int64_t ld, int64_t len, int64_t order,
+                                       int64_t *out_len, void *stream);
+PMLG_API int pmlg_mat_poly_to_poly_mat(pmlg_ctx *ctx, uint64_t *out, int64_t out_cap, const uint64_t *in,
+                                       int64_t r, int64_t c, int64_t len, int64_t order, void *stream);
+
 /* ---------------------------------------------------------------------- */
 /* L1: modular dot products and multimodular reduction / CRT               */
 /* ---------------------------------------------------------------------- */

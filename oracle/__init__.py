@@ -63,6 +63,10 @@ def lib():
             "orc_kernel_zls": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
                                            C.c_int64, C.c_uint64, C.c_int]),
             "orc_free": (None, [C.c_void_p]),
+            "orc_poly_mat_to_mat_poly": (C.c_int64, [_u64p, C.c_int64, _u64p, C.c_int64, C.c_int64, C.c_int64,
+                                                     C.c_int64, C.c_int64]),
+            "orc_mat_poly_to_poly_mat": (None, [_u64p, C.c_int64, _u64p, C.c_int64, C.c_int64, C.c_int64,
+                                                C.c_int64]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -271,6 +275,31 @@ def row_degrees_and_pivots(ker: np.ndarray, shift):
         rdeg.append(best if best is not None else None)
         piv.append(bj)
     return rdeg, piv
+
+
+# ---- layout conversions ----------------------------------------------------
+
+def poly_mat_to_mat_poly(P: np.ndarray, order: int, out_cap: int = None):
+    """(r, c, len) entry-major -> (out_cap, r, c) coefficient-major, truncated at
+    order; returns (array, normalised length)."""
+    P = _c64(P)
+    r, c, ln = P.shape
+    K = min(order, ln)
+    out_cap = K if out_cap is None else out_cap
+    out = np.zeros((max(out_cap, 0), r, c), dtype=np.uint64)
+    L = int(lib().orc_poly_mat_to_mat_poly(_p64(out), out_cap, _p64(P), r, c, ln, ln, order))
+    return out, L
+
+
+def mat_poly_to_poly_mat(M: np.ndarray, order: int, out_cap: int = None):
+    """(len, r, c) coefficient-major -> (r, c, out_cap) entry-major, truncated at order."""
+    M = _c64(M)
+    ln, r, c = M.shape
+    K = min(order, ln)
+    out_cap = K if out_cap is None else out_cap
+    out = np.zeros((r, c, max(out_cap, 0)), dtype=np.uint64)
+    lib().orc_mat_poly_to_poly_mat(_p64(out), out_cap, _p64(M), r, c, ln, order)
+    return out
 
 
 # ---- dot products, CRT ------------------------------------------------------

@@ -1471,3 +1471,38 @@ void orc_free(void *ptr)
 {
     free(ptr);
 }
+
+/* ------------------------------------------------------------------ */
+/* layout conversions (nmod_mat_poly_set_from.c:31-52,                 */
+/* nmod_poly_mat_utils.c:185-210)                                      */
+/* ------------------------------------------------------------------ */
+
+int64_t orc_poly_mat_to_mat_poly(uint64_t *out, int64_t out_cap, const uint64_t *in, int64_t r, int64_t c,
+                                 int64_t ld, int64_t len, int64_t order)
+{
+    const int64_t ne = r * c, K = order < len ? order : len;
+    for (int64_t k = 0; k < out_cap; k++)
+        for (int64_t e = 0; e < ne; e++)
+            out[k * ne + e] = k < K ? in[e * ld + k] : 0;
+    /* normalise: drop trailing zero coefficient matrices */
+    int64_t L = K;
+    while (L > 0)
+    {
+        int nz = 0;
+        for (int64_t e = 0; e < ne && !nz; e++)
+            nz = out[(L - 1) * ne + e] != 0;
+        if (nz)
+            break;
+        L--;
+    }
+    return L;
+}
+
+void orc_mat_poly_to_poly_mat(uint64_t *out, int64_t out_cap, const uint64_t *in, int64_t r, int64_t c,
+                              int64_t len, int64_t order)
+{
+    const int64_t ne = r * c, K = order < len ? order : len;
+    for (int64_t e = 0; e < ne; e++)
+        for (int64_t k = 0; k < out_cap; k++)
+            out[e * out_cap + k] = k < K ? in[k * ne + e] : 0;
+}

@@ -150,6 +150,17 @@ int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *
                        int nthreads);
 void orc_free(void *ptr);
 
+/* ---- layout conversions ---- */
+/* nmod_mat_poly_set_trunc_from_poly_mat (nmod_mat_poly_set_from.c:31-52):
+ * out[k][i][j] = in[(i*c + j)*ld + k] for k < min(order, len), zero up to out_cap;
+ * returns the normalised length (last nonzero coefficient matrix + 1). */
+int64_t orc_poly_mat_to_mat_poly(uint64_t *out, int64_t out_cap, const uint64_t *in, int64_t r, int64_t c,
+                                 int64_t ld, int64_t len, int64_t order);
+/* nmod_poly_mat_set_trunc_from_mat_poly (nmod_poly_mat_utils.c:185-210):
+ * out[(i*c + j)*out_cap + k] = in[k][i][j] for k < min(order, len), zero up to out_cap. */
+void orc_mat_poly_to_poly_mat(uint64_t *out, int64_t out_cap, const uint64_t *in, int64_t r, int64_t c,
+                              int64_t len, int64_t order);
+
 #ifdef __cplusplus
 }
 #endif

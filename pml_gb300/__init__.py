@@ -29,7 +29,8 @@ from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_F16_TC, FORM_INT8_TC, PmlgErro
 __all__ = [
     "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
-    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_kernel", "nmod_vec_dot_product", "nmod32_vec_dot_product",
+    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_kernel",
+    "nmod_mat_poly_set_trunc_from_poly_mat", "nmod_poly_mat_set_trunc_from_mat_poly", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
 ]
 
@@ -256,6 +257,41 @@ def nmod_poly_mat_mbasis(F, order: int, shift, p: int, ctx: Optional[Context] = 
     """nmod_poly_mat_mbasis (approximant_basis.c:18), CUDA tensors only."""
     ctx = _ctx(ctx, F)
     return _approx(ctx.lib.pmlg_mbasis, None, F, order, shift, p, ctx)
+
+
+# ---------------------------------------------------------------------------
+# layout conversions
+# ---------------------------------------------------------------------------
+
+def nmod_mat_poly_set_trunc_from_poly_mat(P, order: int, ctx: Optional[Context] = None, out=None):
+    """Coefficient-major copy (len, r, c) of the entry-major CUDA tensor P (r, c, len),
+    truncated at order (nmod_mat_poly_set_from.c:31).  Returns (out, normalised length)."""
+    import torch
+    _require_cuda(P)
+    ctx = _ctx(ctx, P)
+    r, c, ln = P.shape
+    K = min(order, ln)
+    if out is None:
+        out = torch.empty((K, r, c), dtype=torch.int64, device=P.device)
+    L = C.c_int64(0)
+    ctx.check(ctx.lib.pmlg_poly_mat_to_mat_poly(ctx.handle, _ptr(out), out.shape[0], _ptr(P), r, c, ln, ln, order,
+                                                C.byref(L), _stream_ptr(P)))
+    return out, int(L.value)
+
+
+def nmod_poly_mat_set_trunc_from_mat_poly(M, order: int, ctx: Optional[Context] = None, out=None):
+    """Entry-major copy (r, c, K) of the coefficient-major CUDA tensor M (len, r, c),
+    K = min(order, len) (nmod_poly_mat_utils.c:185)."""
+    import torch
+    _require_cuda(M)
+    ctx = _ctx(ctx, M)
+    ln, r, c = M.shape
+    K = min(order, ln)
+    if out is None:
+        out = torch.empty((r, c, K), dtype=torch.int64, device=M.device)
+    ctx.check(ctx.lib.pmlg_mat_poly_to_poly_mat(ctx.handle, _ptr(out), out.shape[2], _ptr(M), r, c, ln, order,
+                                                _stream_ptr(M)))
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -49,6 +49,8 @@ SIGNATURES = {
     "pmlg_kernel_zls": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_kernel_zls_host": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p,
                                        _vp]),
+    "pmlg_poly_mat_to_mat_poly": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _i64, _i64p, _vp]),
+    "pmlg_mat_poly_to_poly_mat": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp]),
     "pmlg_nmod_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
     "pmlg_nmod32_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
     "pmlg_nmod32_vec_mdot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _i64, _i64, _u64, _vp]),
