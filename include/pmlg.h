@@ -207,6 +207,22 @@ PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap,
                                   int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
                                   int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
 
+/* Truncated inverse: S (device, n x n of capacity order + 1) = A^-1 mod x^order for
+ * A (device, n x n, entry stride alen), from the approximant basis of [A \\ -I] at
+ * order with shift [0, ..., 0, order, ..., order].  *invertible = 1 when A(0) is
+ * invertible (S written), 0 otherwise.  n <= 32, p a prime < 2^30; the stream is
+ * synchronised.  Replaces nmod_poly_mat_inv_trunc
+ * (flint-extras/src/nmod_poly_mat_extra/nmod_poly_mat_dixon.c:32-80). */
+PMLG_API int pmlg_inv_trunc(pmlg_ctx *ctx, uint64_t *S, const uint64_t *A, int64_t n, int64_t alen,
+                            int64_t order, uint64_t p, int *invertible, void *stream);
+/* Dixon lifting: X (device, n x m of capacity xcap >= ceil(sigma / order) * order)
+ * with A X = B mod x^sigma, built one x-adic digit of order coefficients at a time:
+ * S = A^-1 B mod x^order, X += x^(l order) S, B <- (B - A S) div x^order.  *ok = 1, or
+ * 0 when A(0) is singular.  Replaces nmod_poly_mat_dixon (nmod_poly_mat_dixon.c:92-143). */
+PMLG_API int pmlg_dixon(pmlg_ctx *ctx, uint64_t *X, int64_t xcap, const uint64_t *A, const uint64_t *B,
+                        int64_t n, int64_t m, int64_t alen, int64_t blen, int64_t order, int64_t sigma,
+                        uint64_t p, int *ok, void *stream);
+
 /* Layout conversions (device buffers).  Entry-major (nmod_poly_mat): entry (i, j)
  * holds coefficients at [(i*c + j)*ld, (i*c + j)*ld + len).  Coefficient-major
  * (nmod_mat_poly): coefficient k is the r x c matrix at [k*r*c, (k+1)*r*c).

@@ -63,6 +63,9 @@ def lib():
             "orc_kernel_zls": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
                                            C.c_int64, C.c_uint64, C.c_int]),
             "orc_free": (None, [C.c_void_p]),
+            "orc_inv_trunc": (C.c_int, [_u64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
+            "orc_dixon": (C.c_int, [_u64p, _u64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                    C.c_int64, C.c_uint64, C.c_int]),
             "orc_poly_mat_to_mat_poly": (C.c_int64, [_u64p, C.c_int64, _u64p, C.c_int64, C.c_int64, C.c_int64,
                                                      C.c_int64, C.c_int64]),
             "orc_mat_poly_to_poly_mat": (None, [_u64p, C.c_int64, _u64p, C.c_int64, C.c_int64, C.c_int64,
@@ -275,6 +278,29 @@ def row_degrees_and_pivots(ker: np.ndarray, shift):
         rdeg.append(best if best is not None else None)
         piv.append(bj)
     return rdeg, piv
+
+
+# ---- truncated inverse, Dixon lifting --------------------------------------
+
+def inv_trunc(A: np.ndarray, order: int, p: int, nthreads: int = 1):
+    """(S, invertible): S = A^-1 mod x^order, shape (n, n, order + 1) (nmod_poly_mat_dixon.c:32)."""
+    A = _c64(A)
+    n, _, alen = A.shape
+    S = np.zeros((n, n, order + 1), dtype=np.uint64)
+    ok = int(lib().orc_inv_trunc(_p64(S), _p64(A), n, alen, order, p, nthreads))
+    return S, bool(ok)
+
+
+def dixon(A: np.ndarray, B: np.ndarray, order: int, sigma: int, p: int, nthreads: int = 1):
+    """(X, ok): A X = B mod x^sigma by x-adic lifting (nmod_poly_mat_dixon.c:92);
+    X has shape (n, m, ceil(sigma / order) * order)."""
+    A, B = _c64(A), _c64(B)
+    n, _, alen = A.shape
+    _, m, blen = B.shape
+    L = (sigma + order - 1) // order
+    X = np.zeros((n, m, max(L * order, 1)), dtype=np.uint64)
+    ok = int(lib().orc_dixon(_p64(X), _p64(A), _p64(B), n, m, alen, blen, order, sigma, p, nthreads))
+    return X, bool(ok)
 
 
 # ---- layout conversions ----------------------------------------------------

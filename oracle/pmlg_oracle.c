@@ -1506,3 +1506,100 @@ void orc_mat_poly_to_poly_mat(uint64_t *out, int64_t out_cap, const uint64_t *in
         for (int64_t k = 0; k < out_cap; k++)
             out[e * out_cap + k] = k < K ? in[k * ne + e] : 0;
 }
+
+/* ------------------------------------------------------------------ */
+/* truncated inverse and Dixon lifting (nmod_poly_mat_dixon.c)         */
+/* ------------------------------------------------------------------ */
+
+/* nmod_poly_mat_inv_trunc (nmod_poly_mat_dixon.c:32-80): S = A^-1 mod x^order from the
+ * approximant basis of [A \\ -I] at order with shift [0, ..., 0, order, ..., order];
+ * A invertible at x = 0 <=> the bottom-right block of the basis is the identity.
+ * A: n x n, capacity alen; S: n x n, capacity order + 1.  Returns 1 (invertible) or 0. */
+int orc_inv_trunc(uint64_t *S, const uint64_t *A, int64_t n, int64_t alen, int64_t order, uint64_t p,
+                  int nthreads)
+{
+    const int64_t m = 2 * n, hl = alen > 0 ? alen : 1;
+    uint64_t *H = (uint64_t *) calloc((size_t) (m * n * hl + 1), sizeof(uint64_t));
+    for (int64_t i = 0; i < n; i++)
+        for (int64_t j = 0; j < n; j++)
+            memcpy(H + (i * n + j) * hl, A + (i * n + j) * alen, sizeof(uint64_t) * (size_t) alen);
+    for (int64_t i = n; i < m; i++)
+        H[(i * n + (i - n)) * hl] = p - 1;
+    int64_t *shift = (int64_t *) malloc(sizeof(int64_t) * (size_t) m);
+    for (int64_t i = 0; i < m; i++)
+        shift[i] = i < n ? 0 : order;
+    const int64_t cap = order + 1;
+    uint64_t *T = (uint64_t *) calloc((size_t) (m * m * cap + 1), sizeof(uint64_t));
+    orc_pmbasis(T, shift, H, m, n, hl, order, p, 32, nthreads);
+    int is_inv = 1;
+    for (int64_t i = 0; i < n && is_inv; i++)
+        for (int64_t j = 0; j < n && is_inv; j++)
+        {
+            const uint64_t *e = T + ((n + i) * m + (n + j)) * cap;
+            for (int64_t d = 0; d < cap && is_inv; d++)
+                if (e[d] != ((i == j && d == 0) ? 1u : 0u))
+                    is_inv = 0;
+        }
+    if (is_inv)
+        for (int64_t i = 0; i < n; i++)
+            for (int64_t j = 0; j < n; j++)
+                memcpy(S + (i * n + j) * cap, T + ((n + i) * m + j) * cap, sizeof(uint64_t) * (size_t) cap);
+    free(H); free(shift); free(T);
+    return is_inv;
+}
+
+/* nmod_poly_mat_dixon (nmod_poly_mat_dixon.c:92-143): X with A X = B mod x^sigma by
+ * x-adic lifting with the inverse mod x^order.  A: n x n (capacity alen), B: n x m
+ * (capacity blen); X: n x m of capacity L * order, L = ceil(sigma / order), the sum of
+ * the digits x^(l order) S_l.  Returns 1, or 0 when A is not invertible at x = 0. */
+int orc_dixon(uint64_t *X, const uint64_t *A, const uint64_t *B, int64_t n, int64_t m, int64_t alen,
+              int64_t blen, int64_t order, int64_t sigma, uint64_t p, int nthreads)
+{
+    const int64_t ccap = order + 1;
+    uint64_t *Cinv = (uint64_t *) calloc((size_t) (n * n * ccap + 1), sizeof(uint64_t));
+    if (!orc_inv_trunc(Cinv, A, n, alen, order, p, nthreads))
+    {
+        free(Cinv);
+        return 0;
+    }
+    const int64_t L = (sigma + order - 1) / order, xcap = L * order;
+    memset(X, 0, sizeof(uint64_t) * (size_t) (n * m * xcap));
+    /* BB: the current residue, capacity bcap (grows to the largest length it reaches) */
+    int64_t bcap = blen > 0 ? blen : 1;
+    uint64_t *BB = pm_recap(B, n, m, blen, bcap);
+    for (int64_t l = 0; l * order < sigma; l++)
+    {
+        /* S = C * BB mod x^order */
+        const int64_t sl = ccap + bcap - 1;
+        uint64_t *full = (uint64_t *) calloc((size_t) (n * m * sl + 1), sizeof(uint64_t));
+        orc_poly_mat_mul(full, Cinv, BB, n, n, m, ccap, bcap, p, nthreads);
+        uint64_t *S = (uint64_t *) calloc((size_t) (n * m * order + 1), sizeof(uint64_t));
+        for (int64_t e = 0; e < n * m; e++)
+            for (int64_t d = 0; d < order && d < sl; d++)
+                S[e * order + d] = full[e * sl + d];
+        free(full);
+        /* X += x^(l order) S */
+        for (int64_t e = 0; e < n * m; e++)
+            for (int64_t d = 0; d < order; d++)
+                X[e * xcap + l * order + d] = S[e * order + d];
+        /* BB = (BB - A S) div x^order */
+        const int64_t tl = alen + order - 1;
+        uint64_t *AS = (uint64_t *) calloc((size_t) (n * m * tl + 1), sizeof(uint64_t));
+        orc_poly_mat_mul(AS, A, S, n, n, m, alen, order, p, nthreads);
+        const int64_t ncap = (bcap > tl ? bcap : tl) - order > 0 ? (bcap > tl ? bcap : tl) - order : 1;
+        uint64_t *NB = (uint64_t *) calloc((size_t) (n * m * ncap + 1), sizeof(uint64_t));
+        for (int64_t e = 0; e < n * m; e++)
+            for (int64_t d = 0; d < ncap; d++)
+            {
+                const int64_t k = d + order;
+                const uint64_t b = k < bcap ? BB[e * bcap + k] : 0;
+                const uint64_t a = k < tl ? AS[e * tl + k] : 0;
+                NB[e * ncap + d] = b >= a ? b - a : b + p - a;
+            }
+        free(AS); free(S); free(BB);
+        BB = NB;
+        bcap = ncap;
+    }
+    free(BB); free(Cinv);
+    return 1;
+}

@@ -150,6 +150,16 @@ int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *
                        int nthreads);
 void orc_free(void *ptr);
 
+/* ---- truncated inverse and Dixon lifting (nmod_poly_mat_extra/nmod_poly_mat_dixon.c) ---- */
+/* S (n x n, capacity order + 1) = A^-1 mod x^order (:32-80); returns 1, or 0 when A(0) is
+ * singular (S untouched). */
+int orc_inv_trunc(uint64_t *S, const uint64_t *A, int64_t n, int64_t alen, int64_t order, uint64_t p,
+                  int nthreads);
+/* X (n x m, capacity ceil(sigma / order) * order) with A X = B mod x^sigma (:92-143);
+ * returns 1, or 0 when A(0) is singular. */
+int orc_dixon(uint64_t *X, const uint64_t *A, const uint64_t *B, int64_t n, int64_t m, int64_t alen,
+              int64_t blen, int64_t order, int64_t sigma, uint64_t p, int nthreads);
+
 /* ---- layout conversions ---- */
 /* nmod_mat_poly_set_trunc_from_poly_mat (nmod_mat_poly_set_from.c:31-52):
  * out[k][i][j] = in[(i*c + j)*ld + k] for k < min(order, len), zero up to out_cap;

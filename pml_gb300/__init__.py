@@ -30,7 +30,8 @@ __all__ = [
     "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
     "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_kernel",
-    "nmod_mat_poly_set_trunc_from_poly_mat", "nmod_poly_mat_set_trunc_from_mat_poly", "nmod_vec_dot_product", "nmod32_vec_dot_product",
+    "nmod_mat_poly_set_trunc_from_poly_mat", "nmod_poly_mat_set_trunc_from_mat_poly",
+    "nmod_poly_mat_inv_trunc", "nmod_poly_mat_dixon", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
 ]
 
@@ -292,6 +293,39 @@ def nmod_poly_mat_set_trunc_from_mat_poly(M, order: int, ctx: Optional[Context] 
     ctx.check(ctx.lib.pmlg_mat_poly_to_poly_mat(ctx.handle, _ptr(out), out.shape[2], _ptr(M), r, c, ln, order,
                                                 _stream_ptr(M)))
     return out
+
+
+# ---------------------------------------------------------------------------
+# L5: truncated inverse, Dixon lifting
+# ---------------------------------------------------------------------------
+
+def nmod_poly_mat_inv_trunc(A, order: int, p: int, ctx: Optional[Context] = None):
+    """(S, invertible): S = A^-1 mod x^order for the (n, n, len) CUDA tensor A
+    (nmod_poly_mat_dixon.c:32).  S has shape (n, n, order + 1)."""
+    import torch
+    _require_cuda(A)
+    ctx = _ctx(ctx, A)
+    n, _, alen = A.shape
+    S = torch.zeros((n, n, order + 1), dtype=torch.int64, device=A.device)
+    inv = C.c_int(0)
+    ctx.check(ctx.lib.pmlg_inv_trunc(ctx.handle, _ptr(S), _ptr(A), n, alen, order, p, C.byref(inv), _stream_ptr(A)))
+    return S, bool(inv.value)
+
+
+def nmod_poly_mat_dixon(A, B, order: int, sigma: int, p: int, ctx: Optional[Context] = None):
+    """(X, ok): A X = B mod x^sigma by x-adic lifting (nmod_poly_mat_dixon.c:92), CUDA
+    tensors; X has shape (n, m, ceil(sigma / order) * order)."""
+    import torch
+    _require_cuda(A, B)
+    ctx = _ctx(ctx, A)
+    n, _, alen = A.shape
+    _, m, blen = B.shape
+    xcap = max(1, -(-sigma // order) * order)
+    X = torch.zeros((n, m, xcap), dtype=torch.int64, device=A.device)
+    ok = C.c_int(0)
+    ctx.check(ctx.lib.pmlg_dixon(ctx.handle, _ptr(X), xcap, _ptr(A), _ptr(B), n, m, alen, blen, order, sigma, p,
+                                 C.byref(ok), _stream_ptr(A)))
+    return X, bool(ok.value)
 
 
 # ---------------------------------------------------------------------------

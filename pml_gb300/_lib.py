@@ -49,6 +49,9 @@ SIGNATURES = {
     "pmlg_kernel_zls": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_kernel_zls_host": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p,
                                        _vp]),
+    "pmlg_inv_trunc": (C.c_int, [_vp, _vp, _vp, _i64, _i64, _i64, _u64, C.POINTER(C.c_int), _vp]),
+    "pmlg_dixon": (C.c_int, [_vp, _vp, _i64, _vp, _vp, _i64, _i64, _i64, _i64, _i64, _i64, _u64,
+                             C.POINTER(C.c_int), _vp]),
     "pmlg_poly_mat_to_mat_poly": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _i64, _i64p, _vp]),
     "pmlg_mat_poly_to_poly_mat": (C.c_int, [_vp, _vp, _i64, _vp, _i64, _i64, _i64, _i64, _vp]),
     "pmlg_nmod_vec_dot": (C.c_int, [_vp, _vp, _vp, _vp, _i64, _u64, _vp]),
