@@ -413,6 +413,32 @@ def measure_layout(ctx, dev, st, rank, peak_gbs):
     return res
 
 
+def measure_dixon(ctx, dev, st, rank):
+    """x-adic Dixon lifting (nmod_poly_mat_dixon.c:92): A 32x32 of degree 63, B 32x32 of
+    degree 63, digits of 64 coefficients up to sigma = 4096; wall clock around one call
+    (it synchronises) after one warm-up call, and A X = B mod x^sigma checked with the GPU
+    product."""
+    import time
+    import torch
+    import pml_gb300
+    n, m, ln, order, sigma = 32, 32, 64, 64, 4096
+    rng = np.random.default_rng(41 + rank)
+    A = torch.from_numpy(rng.integers(0, P, size=(n, n, ln), dtype=np.uint64).view(np.int64)).to(dev)
+    B = torch.from_numpy(rng.integers(0, P, size=(n, m, ln), dtype=np.uint64).view(np.int64)).to(dev)
+    pml_gb300.nmod_poly_mat_dixon(A, B, order, sigma, P, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    X, ok = pml_gb300.nmod_poly_mat_dixon(A, B, order, sigma, P, ctx=ctx)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    AX = pml_gb300.nmod_poly_mat_multiply(A, X, P, ctx=ctx)[:, :, :sigma]
+    Bs = torch.zeros((n, m, sigma), dtype=torch.int64, device=dev)
+    Bs[:, :, :ln] = B
+    return {"ms": ms, "invertible": ok, "AX_equals_B_mod_x_sigma": bool(torch.equal(AX, Bs)),
+            "config": "Dixon lifting, A and B 32x32 of degree 63, digits of 64, sigma = 4096, p = 998244353",
+            "timing": "wall clock around one call after one warm-up call"}
+
+
 def run_pml(args):
     import torch
     rank, world, local = dist_env()
@@ -593,6 +619,7 @@ def run_pml(args):
         "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
         "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
         "layout_conversion": measure_layout(ctx, dev, st, rank, peaks.get("hbm_gbs")),
+        "dixon": measure_dixon(ctx, dev, st, rank),
     }
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)
