@@ -181,6 +181,15 @@ PMLG_API int pmlg_pmbasis(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, i
 PMLG_API int pmlg_mbasis(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
                          const uint64_t *F, int64_t m, int64_t n, int64_t flen, int64_t order,
                          uint64_t p, int64_t *appbas_len, void *stream);
+/* Shifted Popov approximant basis (the canonical one): pmbasis with shift s, pmbasis
+ * again with shift s - rdeg_s, and the product by the inverse of the second basis'
+ * row leading matrix.  Same buffers and conventions as pmlg_pmbasis; shift out: the
+ * s-row degree.  Replaces popov_pmbasis
+ * (ntl-extras/mat_lzz_pX_extra/src/mat_lzz_pX_pmbasis.cpp:1527-1557), which
+ * flint-extras lists as a TODO (nmod_poly_mat_approximant.h:337-348). */
+PMLG_API int pmlg_popov_pmbasis(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
+                                const uint64_t *F, int64_t m, int64_t n, int64_t flen, int64_t order,
+                                uint64_t p, int64_t *appbas_len, void *stream);
 /* Host-buffer form of pmlg_pmbasis. */
 PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_cap, int64_t *shift,
                                const uint64_t *F, int64_t m, int64_t n, int64_t flen,

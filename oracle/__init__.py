@@ -63,6 +63,8 @@ def lib():
             "orc_kernel_zls": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
                                            C.c_int64, C.c_uint64, C.c_int]),
             "orc_free": (None, [C.c_void_p]),
+            "orc_popov_pmbasis": (C.c_int64, [_u64p, _i64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
+                                              C.c_uint64, C.c_int]),
             "orc_inv_trunc": (C.c_int, [_u64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
             "orc_dixon": (C.c_int, [_u64p, _u64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                     C.c_int64, C.c_uint64, C.c_int]),
@@ -278,6 +280,41 @@ def row_degrees_and_pivots(ker: np.ndarray, shift):
         rdeg.append(best if best is not None else None)
         piv.append(bj)
     return rdeg, piv
+
+
+# ---- shifted Popov approximant basis ---------------------------------------
+
+def popov_pmbasis(F: np.ndarray, order: int, shift, p: int, nthreads: int = 1):
+    """(appbas, rdeg): the shift-Popov approximant basis (popov_pmbasis,
+    mat_lzz_pX_pmbasis.cpp:1527) and its shifted row degree."""
+    F = _c64(F)
+    m, n, flen = F.shape
+    sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+    out = np.zeros((m, m, order + 1), dtype=np.uint64)
+    L = int(lib().orc_popov_pmbasis(_p64(out), _pi64(sh), _p64(F), m, n, flen, order, p, nthreads))
+    return out[:, :, :max(L, 1)], sh
+
+
+def is_popov(P: np.ndarray, shift) -> bool:
+    """Shift-Popov form (row-wise): pivots on the diagonal (the rightmost entry reaching
+    the shifted row degree), monic pivots, and in every column the pivot of strictly
+    largest degree."""
+    m = P.shape[0]
+    rdeg, piv = row_degrees_and_pivots(P, shift)
+    if list(piv) != list(range(m)):
+        return False
+    L = P.shape[2]
+    deg = np.full((m, m), -1, dtype=np.int64)
+    nz = P != 0
+    for d in range(L):
+        deg[nz[:, :, d]] = d
+    for j in range(m):
+        if P[j, j, deg[j, j]] != 1:
+            return False
+        for i in range(m):
+            if i != j and deg[i, j] >= deg[j, j]:
+                return False
+    return True
 
 
 # ---- truncated inverse, Dixon lifting --------------------------------------

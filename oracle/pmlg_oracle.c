@@ -1603,3 +1603,91 @@ int orc_dixon(uint64_t *X, const uint64_t *A, const uint64_t *B, int64_t n, int6
     free(BB); free(Cinv);
     return 1;
 }
+
+/* ------------------------------------------------------------------ */
+/* shifted Popov approximant basis: popov_pmbasis                      */
+/* (ntl-extras/mat_lzz_pX_extra/src/mat_lzz_pX_pmbasis.cpp:1527-1557;  */
+/* the TODO of flint-extras nmod_poly_mat_approximant.h:337-348)       */
+/* ------------------------------------------------------------------ */
+
+/* the t-row leading matrix of P (m x m, capacity cap): row i holds the coefficients of
+ * degree rdeg_t(i) - t[j] of its entries (zero where that degree is out of range) */
+static void row_leading_matrix(uint64_t *lm, const uint64_t *P, int64_t m, int64_t cap, const int64_t *t)
+{
+    for (int64_t i = 0; i < m; i++)
+    {
+        int64_t rd = INT64_MIN;
+        for (int64_t j = 0; j < m; j++)
+        {
+            const int64_t d = poly_deg(P + (i * m + j) * cap, cap);
+            if (d >= 0 && d + t[j] > rd)
+                rd = d + t[j];
+        }
+        for (int64_t j = 0; j < m; j++)
+        {
+            const int64_t k = rd == INT64_MIN ? -1 : rd - t[j];
+            lm[i * m + j] = (k >= 0 && k < cap) ? P[(i * m + j) * cap + k] : 0;
+        }
+    }
+}
+
+int64_t orc_popov_pmbasis(uint64_t *appbas, int64_t *shift, const uint64_t *F, int64_t m, int64_t n,
+                          int64_t flen, int64_t order, uint64_t p, int nthreads)
+{
+    const int64_t cap = order + 1;
+    /* first call: the s-row degree */
+    int64_t *rdeg = (int64_t *) malloc(sizeof(int64_t) * (size_t) m);
+    int64_t *pshift = (int64_t *) malloc(sizeof(int64_t) * (size_t) m);
+    int64_t *t = (int64_t *) malloc(sizeof(int64_t) * (size_t) m);
+    memcpy(rdeg, shift, sizeof(int64_t) * (size_t) m);
+    orc_pmbasis(appbas, rdeg, F, m, n, flen, order, p, 32, nthreads);
+    /* second call with shift s - rdeg_s = minus the pivot degrees */
+    for (int64_t i = 0; i < m; i++)
+    {
+        pshift[i] = shift[i] - rdeg[i];
+        t[i] = pshift[i];
+        shift[i] = rdeg[i];
+    }
+    orc_pmbasis(appbas, pshift, F, m, n, flen, order, p, 32, nthreads);
+    /* appbas <- lmat^-1 appbas, lmat its t-row leading matrix */
+    uint64_t *aug = (uint64_t *) calloc((size_t) (m * 2 * m), sizeof(uint64_t));
+    uint64_t *lm = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (m * m));
+    row_leading_matrix(lm, appbas, m, cap, t);
+    for (int64_t i = 0; i < m; i++)
+    {
+        for (int64_t j = 0; j < m; j++)
+            aug[i * 2 * m + j] = lm[i * m + j];
+        aug[i * 2 * m + m + i] = 1;
+    }
+    const int64_t rk = orc_nmod_mat_rref(aug, m, 2 * m, p);
+    int64_t L = 0;
+    if (rk == m)
+    {
+        uint64_t *inv = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (m * m));
+        for (int64_t i = 0; i < m; i++)
+            for (int64_t j = 0; j < m; j++)
+                inv[i * m + j] = aug[i * 2 * m + m + j];
+        uint64_t *out = (uint64_t *) calloc((size_t) (m * m * cap), sizeof(uint64_t));
+        uint64_t *col = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) m);
+        for (int64_t j = 0; j < m; j++)
+            for (int64_t d = 0; d < cap; d++)
+            {
+                for (int64_t k = 0; k < m; k++)
+                    col[k] = appbas[(k * m + j) * cap + d];
+                for (int64_t i = 0; i < m; i++)
+                {
+                    u128 acc = 0;
+                    for (int64_t k = 0; k < m; k++)
+                        acc += (u128) inv[i * m + k] * col[k];
+                    out[(i * m + j) * cap + d] = (uint64_t) (acc % p);
+                }
+            }
+        memcpy(appbas, out, sizeof(uint64_t) * (size_t) (m * m * cap));
+        free(out); free(col); free(inv);
+        L = orc_pm_max_length(appbas, m, m, cap);
+    }
+    else
+        L = -1;    /* cannot happen for an approximant basis: its leading matrix is invertible */
+    free(aug); free(lm); free(rdeg); free(pshift); free(t);
+    return L;
+}

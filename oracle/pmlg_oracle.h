@@ -150,6 +150,14 @@ int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *
                        int nthreads);
 void orc_free(void *ptr);
 
+/* ---- shifted Popov approximant basis ---- */
+/* popov_pmbasis (ntl-extras/mat_lzz_pX_extra/src/mat_lzz_pX_pmbasis.cpp:1527-1557):
+ * pmbasis with shift s, then with shift s - rdeg_s, then the product by the inverse of
+ * the second basis' row leading matrix.  appbas: m x m, capacity order + 1; shift: in s,
+ * out the s-row degree.  Returns appbas' length. */
+int64_t orc_popov_pmbasis(uint64_t *appbas, int64_t *shift, const uint64_t *F, int64_t m, int64_t n,
+                          int64_t flen, int64_t order, uint64_t p, int nthreads);
+
 /* ---- truncated inverse and Dixon lifting (nmod_poly_mat_extra/nmod_poly_mat_dixon.c) ---- */
 /* S (n x n, capacity order + 1) = A^-1 mod x^order (:32-80); returns 1, or 0 when A(0) is
  * singular (S untouched). */

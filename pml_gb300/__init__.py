@@ -29,7 +29,7 @@ from ._lib import FORM_AUTO, FORM_CUDA_CORE, FORM_F16_TC, FORM_INT8_TC, PmlgErro
 __all__ = [
     "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
-    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_kernel",
+    "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_popov_pmbasis", "nmod_poly_mat_kernel",
     "nmod_mat_poly_set_trunc_from_poly_mat", "nmod_poly_mat_set_trunc_from_mat_poly",
     "nmod_poly_mat_inv_trunc", "nmod_poly_mat_dixon", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
@@ -252,6 +252,13 @@ def nmod_poly_mat_pmbasis(F, order: int, shift, p: int, ctx: Optional[Context] =
     (approximant_basis.c:33).  appbas has shape (m, m, length)."""
     ctx = _ctx(ctx, F)
     return _approx(ctx.lib.pmlg_pmbasis, ctx.lib.pmlg_pmbasis_host, F, order, shift, p, ctx)
+
+
+def nmod_poly_mat_popov_pmbasis(F, order: int, shift, p: int, ctx: Optional[Context] = None):
+    """(appbas, shifted row degree): the shift-Popov approximant basis, canonical
+    (popov_pmbasis, mat_lzz_pX_pmbasis.cpp:1527), CUDA tensors only."""
+    ctx = _ctx(ctx, F)
+    return _approx(ctx.lib.pmlg_popov_pmbasis, None, F, order, shift, p, ctx)
 
 
 def nmod_poly_mat_mbasis(F, order: int, shift, p: int, ctx: Optional[Context] = None):

@@ -16,8 +16,6 @@
 
 namespace pmlg {
 
-namespace {
-
 // length (index of the last nonzero coefficient + 1) of every entry: one block per entry
 __global__ void entry_lengths_kernel(const uint64_t *__restrict__ P, int64_t cap, int *__restrict__ out)
 {
@@ -34,6 +32,23 @@ __global__ void entry_lengths_kernel(const uint64_t *__restrict__ P, int64_t cap
         out[blockIdx.x] = best;
     }
 }
+
+int entry_lengths(pmlg_ctx *ctx, const uint64_t *P, int64_t nent, int64_t cap, int *d_out, std::vector<int> &len,
+                  cudaStream_t st)
+{
+    len.assign((size_t)nent, 0);
+    if (nent == 0) return PMLG_OK;
+    prof_begin(ctx, "entry_lengths", st);
+    entry_lengths_kernel<<<(unsigned)nent, 128, 0, st>>>(P, cap, d_out);
+    prof_end(ctx, st);
+    count_launch(ctx);
+    PMLG_CUDA_TRY(cudaGetLastError());
+    PMLG_CUDA_TRY(cudaMemcpyAsync(len.data(), d_out, (size_t)nent * sizeof(int), cudaMemcpyDeviceToHost, st));
+    PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+    return PMLG_OK;
+}
+
+namespace {
 
 // a polynomial matrix in device memory: entry (i, j) at a + (i * c + j) * cap
 struct DevPm
@@ -76,14 +91,7 @@ class Kzls
             PMLG_CUDA_TRY(cudaMallocAsync((void **)&d_len_, (size_t)ne * sizeof(int), st_));
             len_cap_ = ne;
         }
-        prof_begin(ctx, "entry_lengths", st_);
-        entry_lengths_kernel<<<(unsigned)ne, 128, 0, st_>>>(P.a, P.cap, d_len_);
-        prof_end(ctx, st_);
-        count_launch(ctx);
-        PMLG_CUDA_TRY(cudaGetLastError());
-        PMLG_CUDA_TRY(cudaMemcpyAsync(len.data(), d_len_, (size_t)ne * sizeof(int), cudaMemcpyDeviceToHost, st_));
-        PMLG_CUDA_TRY(cudaStreamSynchronize(st_));
-        return PMLG_OK;
+        return entry_lengths(ctx, P.a, ne, P.cap, d_len_, len, st_);
     }
     int max_length(const DevPm &P, int64_t *L)
     {

@@ -3,6 +3,8 @@
 #pragma once
 #include "pmlg_internal.cuh"
 
+#include <vector>
+
 namespace pmlg {
 
 // One product job in device memory.  Coefficients [lo, lo + cnt) of the
@@ -49,5 +51,10 @@ int poly_mat_mulmid_device(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, cons
 int pmbasis_device(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *shift, const uint64_t *F,
                    int64_t m, int64_t n, int64_t flen, int64_t order, uint64_t p, int64_t *len,
                    cudaStream_t st);
+
+// Length (last nonzero coefficient + 1) of each of nent entries of capacity cap, into
+// len on the host (d_out: nent ints of device scratch; synchronises the stream).
+int entry_lengths(pmlg_ctx *ctx, const uint64_t *P, int64_t nent, int64_t cap, int *d_out, std::vector<int> &len,
+                  cudaStream_t st);
 
 }  // namespace pmlg
