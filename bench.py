@@ -439,6 +439,31 @@ def measure_dixon(ctx, dev, st, rank):
             "timing": "wall clock around one call after one warm-up call"}
 
 
+def measure_popov(ctx, dev, st, rank):
+    """Shift-Popov approximant basis of a 64x32 matrix at order 1024, zero shift
+    (popov_pmbasis: two pmbasis calls and the leading-matrix normalisation); wall clock
+    around one call (it synchronises) after one warm-up call."""
+    import time
+    import torch
+    import pml_gb300
+    m, n, order = 64, 32, 1024
+    rng = np.random.default_rng(51 + rank)
+    F = torch.from_numpy(rng.integers(0, P, size=(m, n, order), dtype=np.uint64).view(np.int64)).to(dev)
+    pml_gb300.nmod_poly_mat_popov_pmbasis(F, order, [0] * m, P, ctx=ctx)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ab, sh = pml_gb300.nmod_poly_mat_popov_pmbasis(F, order, [0] * m, P, ctx=ctx)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    t0 = time.perf_counter()
+    pml_gb300.nmod_poly_mat_pmbasis(F, order, [0] * m, P, ctx=ctx)
+    torch.cuda.synchronize()
+    ms_pm = (time.perf_counter() - t0) * 1e3
+    return {"ms": ms, "pmbasis_ms": ms_pm, "rdeg_sum": int(sum(sh)), "length": int(ab.shape[2]),
+            "config": "shift-Popov approximant basis of a 64x32 matrix at order 1024, zero shift, p = 998244353",
+            "timing": "wall clock around one call after one warm-up call"}
+
+
 def run_pml(args):
     import torch
     rank, world, local = dist_env()
@@ -620,6 +645,7 @@ def run_pml(args):
         "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
         "layout_conversion": measure_layout(ctx, dev, st, rank, peaks.get("hbm_gbs")),
         "dixon": measure_dixon(ctx, dev, st, rank),
+        "popov_pmbasis": measure_popov(ctx, dev, st, rank),
     }
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)
