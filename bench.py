@@ -607,7 +607,7 @@ def run_pml(args):
     h2d = 2 * R * K * LEN * 8
     d2h = R * C * (2 * LEN - 1) * 8
 
-    # pmbasis 64x32, order 8192, both forms (one warm-up call, one timed call each)
+    # pmbasis 64x32, order 8192, every form (one warm-up call, then the median of three timed calls)
     pm = None
     if not args.no_pmbasis:
         rng = np.random.default_rng(7 + rank)
@@ -619,10 +619,14 @@ def run_pml(args):
             ctx.set_form(form)
             pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
             torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            ab, sh = pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
-            torch.cuda.synchronize()
-            pm[name + "_ms"] = ranks_max((time.perf_counter() - t0) * 1e3)
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                ab, sh = pml_gb300.nmod_poly_mat_pmbasis(dF, PM_ORDER, [0] * PM_M, P, ctx=ctx)
+                torch.cuda.synchronize()
+                ts.append((time.perf_counter() - t0) * 1e3)
+            pm[name + "_ms"] = ranks_max(sorted(ts)[1])
+            pm[name + "_ms_min"] = ranks_max(min(ts))
             outs[name] = (ab, sh)
         ctx.set_profiling(True)
         ctx.set_form(HEAD)
@@ -635,7 +639,7 @@ def run_pml(args):
         pm["speedup_f16_tc_vs_cuda_core"] = pm["cuda_core_ms"] / pm["f16_tc_ms"]
         pm["speedup_int8_tc_vs_cuda_core"] = pm["cuda_core_ms"] / pm["int8_tc_ms"]
         pm["config"] = "pmbasis 64x32, order 8192, zero shift, p = 998244353, uniform coefficients"
-        pm["timing"] = "wall clock around one call (it synchronises internally), after one warm-up call"
+        pm["timing"] = "median of three calls, wall clock around each (it synchronises internally), after one warm-up call"
 
     # the two other GPU workloads of the benchmark set: the pointwise contraction alone and the
     # batched uneven products (every form, CUDA events around each call)
