@@ -56,10 +56,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the pointwise-batch and batched-uneven measurements")
-    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven"], default=None,
+    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven", "kernel", "layout"],
+                    default=None,
                     help="run one product per form (or one pmbasis at order 1024, one 4096-product "
-                         "pointwise batch per form, one batched-uneven call with the FP16 form) and exit: "
-                         "the small cases for kernel captures")
+                         "pointwise batch per form, one batched-uneven call with the FP16 form, one kernel "
+                         "basis of a 64x32 degree-255 matrix, one layout conversion each way at 64x64 x 4096) "
+                         "and exit: the small cases for kernel captures")
     return ap.parse_args()
 
 
@@ -91,6 +93,19 @@ def run_profile_case(args):
         r = measure_batched_uneven(ctx, torch.device("cuda", 0), torch.cuda.current_stream(),
                                    (("f16_tc", pml_gb300.FORM_F16_TC),), 0)
         print(json.dumps({"profile_case": "uneven", "ms": r["f16_tc_ms"], "launches": ctx.launches}))
+    elif args.profile_case == "kernel":
+        rng = np.random.default_rng(21)
+        F = torch.from_numpy(rng.integers(0, P, size=(64, 32, 256), dtype=np.uint64).view(np.int64)).cuda()
+        ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel(F, [0] * 64, P, ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "kernel", "nullity": int(ker.shape[0]), "launches": ctx.launches}))
+    elif args.profile_case == "layout":
+        rng = np.random.default_rng(31)
+        Pm = torch.from_numpy(rng.integers(0, P, size=(64, 64, 4096), dtype=np.uint64).view(np.int64)).cuda()
+        M, L = pml_gb300.nmod_mat_poly_set_trunc_from_poly_mat(Pm, 4096, ctx=ctx)
+        Q = pml_gb300.nmod_poly_mat_set_trunc_from_mat_poly(M, 4096, ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "layout", "exact": bool(torch.equal(Pm, Q)), "launches": ctx.launches}))
     else:
         rng = np.random.default_rng(7)
         F = rng.integers(0, P, size=(PM_M, PM_N, 1024), dtype=np.uint64)
