@@ -56,3 +56,21 @@ def test_no_cpu_fallback_in_package():
     for f in (ROOT / "pml_gb300").rglob("*.py"):
         src = f.read_text()
         assert "import oracle" not in src and "from oracle" not in src, f
+
+
+def test_follow_on_entry_points_reject_bad_arguments_without_gpu():
+    """The kernel-basis, Popov, truncated-inverse, Dixon and layout entry points
+    check their arguments before touching a device: a null context is EINVAL."""
+    import ctypes as C
+    from pml_gb300 import _lib
+    L = _lib.load()
+    i64 = C.c_int64(0)
+    ic = C.c_int(0)
+    assert L.pmlg_kernel_zls(None, None, 1, C.byref(i64), None, None, None, 1, 1, 1, 7, C.byref(i64), None) == 1
+    assert L.pmlg_kernel_zls_host(None, None, 1, C.byref(i64), None, None, None, 1, 1, 1, 7, C.byref(i64),
+                                  None) == 1
+    assert L.pmlg_popov_pmbasis(None, None, 2, None, None, 1, 1, 1, 1, 7, None, None) == 1
+    assert L.pmlg_inv_trunc(None, None, None, 1, 1, 4, 7, C.byref(ic), None) == 1
+    assert L.pmlg_dixon(None, None, 8, None, None, 1, 1, 1, 1, 4, 8, 7, C.byref(ic), None) == 1
+    assert L.pmlg_poly_mat_to_mat_poly(None, None, 4, None, 1, 1, 4, 4, 4, None, None) == 1
+    assert L.pmlg_mat_poly_to_poly_mat(None, None, 4, None, 1, 1, 4, 4, None) == 1

@@ -71,3 +71,32 @@ def test_status_codes_and_recovery(ctx):
     ab, sh = pml_gb300.nmod_poly_mat_pmbasis(F, 16, [0] * 4, P998, ctx=ctx)
     ref, rsh = oracle.pmbasis(to_host(F), 16, [0] * 4, P998)
     assert list(sh) == list(rsh) and np.array_equal(to_host(ab), ref)
+
+
+def test_follow_on_status_codes(ctx):
+    """Limits and moduli of the kernel-basis, Popov, truncated-inverse, Dixon and
+    layout entry points come back as status codes; the context keeps working."""
+    import ctypes as C
+    import torch
+    L = ctx.lib
+    st = _stream()
+    i64, nul, ic = C.c_int64(0), C.c_int64(0), C.c_int(0)
+    sh = (C.c_int64 * 65)()
+    piv = (C.c_int64 * 65)()
+    P = torch.zeros((65, 2, 4), dtype=torch.int64, device="cuda")
+    K = torch.zeros((65, 65, 8), dtype=torch.int64, device="cuda")
+    # kernel basis: m > 64, a composite modulus
+    assert L.pmlg_kernel_zls(ctx.handle, K.data_ptr(), 8, C.byref(i64), piv, sh, P.data_ptr(), 65, 2, 4, P998,
+                             C.byref(nul), st) == EUNSUP
+    assert L.pmlg_kernel_zls(ctx.handle, K.data_ptr(), 8, C.byref(i64), piv, sh, P.data_ptr(), 4, 2, 4, P998 - 1,
+                             C.byref(nul), st) == EBADMOD
+    # truncated inverse and Dixon: n > 32; Dixon output shorter than ceil(sigma / order) * order
+    assert L.pmlg_inv_trunc(ctx.handle, K.data_ptr(), P.data_ptr(), 33, 1, 4, P998, C.byref(ic), st) == EUNSUP
+    assert L.pmlg_dixon(ctx.handle, K.data_ptr(), 7, P.data_ptr(), P.data_ptr(), 2, 1, 1, 1, 4, 8, P998,
+                        C.byref(ic), st) == EINVAL
+    # Popov basis: a capacity below order + 1; layout: an output shorter than the truncation
+    assert L.pmlg_popov_pmbasis(ctx.handle, K.data_ptr(), 4, sh, P.data_ptr(), 4, 2, 4, 4, P998, None,
+                                st) == EINVAL
+    assert L.pmlg_poly_mat_to_mat_poly(ctx.handle, K.data_ptr(), 3, P.data_ptr(), 4, 2, 4, 4, 4, None,
+                                       st) == EINVAL
+    assert ctx.lib.pmlg_ctx_device_status(ctx.handle, st) == 0
