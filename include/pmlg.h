@@ -58,6 +58,24 @@ enum pmlg_form
                                  partial sums below 2^22 so every step is exact) */
 };
 
+/* Orientations and forms of polynomial matrices, with the values of the reference's
+ * orientation_t and poly_mat_form_t (flint-extras/src/nmod_poly_mat_forms.h:57-104). */
+enum pmlg_orientation
+{
+    PMLG_COL_UPPER = 0,
+    PMLG_COL_LOWER = 1,
+    PMLG_ROW_UPPER = 2,
+    PMLG_ROW_LOWER = 3
+};
+enum pmlg_poly_mat_form
+{
+    PMLG_NONE = 0,
+    PMLG_REDUCED = 1,
+    PMLG_WEAK_POPOV = 2,
+    PMLG_ORD_WEAK_POPOV = 3,
+    PMLG_POPOV = 4
+};
+
 /* ---------------------------------------------------------------------- */
 /* context                                                                 */
 /* ---------------------------------------------------------------------- */
@@ -211,6 +229,23 @@ PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_c
 PMLG_API int pmlg_kernel_zls(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
                              int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
                              int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
+/* nmod_poly_mat_kernel_via_approx (kernel.c:146-227): one approximant basis at the
+ * order min(m, n) deg + amp(shift) + deg + 1, whose rows of small shifted degree are
+ * the kernel rows.  Same buffers and conventions as pmlg_kernel_zls. */
+PMLG_API int pmlg_kernel_via_approx(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
+                                    int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
+                                    int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream);
+/* nmod_poly_mat_kernel (kernel.c:26-144): the kernel of the r x c matrix pmat (device,
+ * entry stride plen) in the given orientation, form at most PMLG_ORD_WEAK_POPOV
+ * (PMLG_EUNSUP otherwise, where the reference throws).  Left kernels (PMLG_ROW_*):
+ * ker is r x r with the basis in its first *nullity rows; right kernels (PMLG_COL_*):
+ * ker is c x c with the basis in its first *nullity columns; the other rows / columns
+ * are zero.  shift (host) may be NULL for the default (row or column degrees, zero
+ * for zero rows or columns); otherwise it is in/out as in the reference.  pivind
+ * (host): the pivot indices.  ker_cap / *ker_len as in pmlg_kernel_zls. */
+PMLG_API int pmlg_kernel(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len, int64_t *pivind,
+                         int64_t *shift, const uint64_t *pmat, int64_t r, int64_t c, int64_t plen,
+                         uint64_t p, int form, int orient, int64_t *nullity, void *stream);
 /* Host-buffer form of pmlg_kernel_zls (ker and pmat in host memory). */
 PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
                                   int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,

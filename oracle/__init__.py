@@ -63,6 +63,10 @@ def lib():
             "orc_kernel_zls": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
                                            C.c_int64, C.c_uint64, C.c_int]),
             "orc_free": (None, [C.c_void_p]),
+            "orc_kernel_via_approx": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64,
+                                                  C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
+            "orc_kernel": (C.c_int64, [C.POINTER(_u64p), _i64p, _i64p, _i64p, _u64p, C.c_int64, C.c_int64,
+                                       C.c_int64, C.c_uint64, C.c_int, C.c_int]),
             "orc_popov_pmbasis": (C.c_int64, [_u64p, _i64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                               C.c_uint64, C.c_int]),
             "orc_inv_trunc": (C.c_int, [_u64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
@@ -258,6 +262,48 @@ def kernel_zls(pmat: np.ndarray, shift, p: int, nthreads: int = 1):
     lib().orc_free(C.cast(kp, C.c_void_p))
     ker = flat.reshape(m, m, L.value)[:nul] if m else np.zeros((0, 0, 1), dtype=np.uint64)
     return ker, piv[:nul].copy(), sh[:nul].copy(), nul
+
+
+def _take(kp, shape):
+    n = int(np.prod(shape))
+    flat = np.ctypeslib.as_array(kp, shape=(max(n, 1),)).copy()[:n] if n else np.zeros(0, dtype=np.uint64)
+    lib().orc_free(C.cast(kp, C.c_void_p))
+    return flat.reshape(shape)
+
+
+def kernel_via_approx(pmat: np.ndarray, shift, p: int, nthreads: int = 1):
+    """nmod_poly_mat_kernel_via_approx (kernel.c:146-227): (ker rows, pivind, rdeg, nullity)."""
+    P = _c64(pmat)
+    m, n, plen = P.shape
+    sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+    piv = np.zeros(max(m, 1), dtype=np.int64)
+    kp, L = _u64p(), C.c_int64(0)
+    nul = int(lib().orc_kernel_via_approx(C.byref(kp), C.byref(L), _pi64(piv), _pi64(sh), _p64(P), m, n, plen, p,
+                                          nthreads))
+    ker = _take(kp, (m, m, L.value))[:nul]
+    return ker, piv[:nul].copy(), sh[:nul].copy(), nul
+
+
+ORIENT = {"COL_UPPER": 0, "COL_LOWER": 1, "ROW_UPPER": 2, "ROW_LOWER": 3}
+
+
+def kernel(pmat: np.ndarray, shift, p: int, orient: str = "ROW_LOWER", nthreads: int = 1):
+    """nmod_poly_mat_kernel (kernel.c:26-144), ORD_WEAK_POPOV: (ker, pivind, shift_out,
+    nullity).  Left kernels return the (nullity, r, L) rows; right kernels the
+    (c, nullity, L) columns.  shift None: the default row / column degrees."""
+    P = _c64(pmat)
+    r, c, plen = P.shape
+    o = ORIENT[orient]
+    left = o >= 2
+    m = r if left else c
+    sh = None if shift is None else np.ascontiguousarray(shift, dtype=np.int64).copy()
+    piv = np.zeros(max(m, 1), dtype=np.int64)
+    kp, L = _u64p(), C.c_int64(0)
+    nul = int(lib().orc_kernel(C.byref(kp), C.byref(L), _pi64(piv), _pi64(sh) if sh is not None else None, _p64(P),
+                               r, c, plen, p, o, nthreads))
+    K = _take(kp, (m, m, L.value))
+    ker = K[:nul] if left else K[:, :nul]
+    return ker, piv[:nul].copy(), (sh[:nul].copy() if sh is not None else None), nul
 
 
 def row_degrees_and_pivots(ker: np.ndarray, shift):

@@ -1691,3 +1691,171 @@ int64_t orc_popov_pmbasis(uint64_t *appbas, int64_t *shift, const uint64_t *F, i
     free(aug); free(lm); free(rdeg); free(pshift); free(t);
     return L;
 }
+
+/* ------------------------------------------------------------------ */
+/* nmod_poly_mat_kernel_via_approx (kernel.c:146-227) and the          */
+/* orientation interface nmod_poly_mat_kernel (kernel.c:26-144)        */
+/* ------------------------------------------------------------------ */
+
+int64_t orc_kernel_via_approx(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift,
+                              const uint64_t *pmat, int64_t m, int64_t n, int64_t plen, uint64_t p,
+                              int nthreads)
+{
+    const int64_t cap0 = plen > 0 ? plen : 1;
+    const int64_t d = orc_pm_max_length(pmat, m, n, cap0) - 1;
+    *klen = 1;
+    if (d == -1)
+    {
+        uint64_t *K = (uint64_t *) calloc((size_t) (m * m + 1), sizeof(uint64_t));
+        for (int64_t i = 0; i < m; i++) { K[i * m + i] = 1; pivind[i] = i; }
+        *ker = K;
+        return m;
+    }
+    if (m == 1)
+    {
+        *ker = (uint64_t *) calloc((size_t) (m * m + 1), sizeof(uint64_t));
+        return 0;
+    }
+    if (m <= n)
+    {
+        /* full row rank of the constant coefficient => empty kernel (:171-184) */
+        uint64_t *c0 = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (m * n));
+        for (int64_t e = 0; e < m * n; e++)
+            c0[e] = pmat[e * cap0];
+        const int64_t r = orc_nmod_mat_rref(c0, m, n, p);
+        free(c0);
+        if (r == m)
+        {
+            *ker = (uint64_t *) calloc((size_t) (m * m + 1), sizeof(uint64_t));
+            return 0;
+        }
+    }
+    int64_t mn = shift[0], amp = shift[0];
+    for (int64_t i = 0; i < m; i++)
+    {
+        const int64_t s = shift[i];
+        pivind[i] = s;
+        if (s < mn) mn = s;
+        else if (s > amp) amp = s;
+    }
+    amp -= mn;
+    const int64_t order = (m < n ? m : n) * d + amp + d + 1;
+    const int64_t cap = order + 1;
+    uint64_t *K = (uint64_t *) calloc((size_t) (m * m * cap + 1), sizeof(uint64_t));
+    orc_pmbasis(K, pivind, pmat, m, n, cap0, order, p, 32, nthreads);
+    int64_t nullity = 0;
+    uint64_t *tmp = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (m * cap));
+    for (int64_t i = 0; i < m; i++)
+    {
+        if (pivind[i] - shift[i] + amp < order - d)
+        {
+            shift[nullity] = pivind[i];
+            pivind[nullity] = i;
+            /* swap rows nullity and i */
+            memcpy(tmp, K + nullity * m * cap, sizeof(uint64_t) * (size_t) (m * cap));
+            memcpy(K + nullity * m * cap, K + i * m * cap, sizeof(uint64_t) * (size_t) (m * cap));
+            memcpy(K + i * m * cap, tmp, sizeof(uint64_t) * (size_t) (m * cap));
+            nullity++;
+        }
+    }
+    free(tmp);
+    /* kernel rows, trimmed; other rows zero */
+    const int64_t L0 = orc_pm_max_length(K, nullity, m, cap);
+    const int64_t L = L0 > 0 ? L0 : 1;
+    uint64_t *out = (uint64_t *) calloc((size_t) (m * m * L + 1), sizeof(uint64_t));
+    for (int64_t e = 0; e < nullity * m; e++)
+        memcpy(out + e * L, K + e * cap, sizeof(uint64_t) * (size_t) L);
+    free(K);
+    *ker = out;
+    *klen = L;
+    return nullity;
+}
+
+/* entry (i, j) of an r x c matrix (capacity cap) -> Q[(j, i)] */
+static uint64_t *pm_transpose(const uint64_t *P, int64_t r, int64_t c, int64_t cap)
+{
+    uint64_t *Q = (uint64_t *) calloc((size_t) (r * c * cap + 1), sizeof(uint64_t));
+    for (int64_t i = 0; i < r; i++)
+        for (int64_t j = 0; j < c; j++)
+            memcpy(Q + (j * r + i) * cap, P + (i * c + j) * cap, sizeof(uint64_t) * (size_t) cap);
+    return Q;
+}
+
+/* nmod_poly_mat_kernel (kernel.c:26-144), form ORD_WEAK_POPOV, orientation orient
+ * (COL_UPPER 0, COL_LOWER 1, ROW_UPPER 2, ROW_LOWER 3).  pmat: r x c, capacity plen.
+ * Left kernels (ROW_*): *ker is r x r with the basis in its first nullity rows; right
+ * kernels (COL_*): *ker is c x c with the basis in its first nullity columns.  shift:
+ * NULL for the default (row / column degrees, zero for zero rows / columns), else
+ * in/out as in the reference.  Returns the nullity. */
+int64_t orc_kernel(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift, const uint64_t *pmat,
+                   int64_t r, int64_t c, int64_t plen, uint64_t p, int orient, int nthreads)
+{
+    const int left = orient == 2 || orient == 3;
+    const int64_t m = left ? r : c, n = left ? c : r, cap0 = plen > 0 ? plen : 1;
+    int64_t *sh = (int64_t *) malloc(sizeof(int64_t) * (size_t) (m > 0 ? m : 1));
+    if (shift)
+        memcpy(sh, shift, sizeof(int64_t) * (size_t) m);
+    else
+        for (int64_t i = 0; i < m; i++)
+        {
+            int64_t mx = 0;
+            for (int64_t j = 0; j < n; j++)
+            {
+                const uint64_t *e = left ? pmat + (i * c + j) * cap0 : pmat + (j * c + i) * cap0;
+                const int64_t dg = poly_deg(e, cap0);
+                if (dg > mx) mx = dg;
+            }
+            sh[i] = mx;
+        }
+    /* the ROW_LOWER problem: transposed for right kernels, rows reversed for *_UPPER / COL_LOWER */
+    uint64_t *M = left ? pm_recap(pmat, r, c, cap0, cap0) : pm_transpose(pmat, r, c, cap0);
+    const int rev = orient == 2 || orient == 1;
+    if (rev)
+    {
+        for (int64_t i = 0; i < m / 2; i++)
+        {
+            for (int64_t j = 0; j < n * cap0; j++)
+            {
+                uint64_t t = M[i * n * cap0 + j];
+                M[i * n * cap0 + j] = M[(m - 1 - i) * n * cap0 + j];
+                M[(m - 1 - i) * n * cap0 + j] = t;
+            }
+            int64_t t = sh[i]; sh[i] = sh[m - 1 - i]; sh[m - 1 - i] = t;
+        }
+    }
+    uint64_t *K = NULL;
+    int64_t L = 1;
+    const int64_t nul = orc_kernel_zls(&K, &L, pivind, sh, M, m, n, cap0, p, nthreads);
+    free(M);
+    if (rev && nul > 0)
+    {
+        /* reverse the kernel rows (and their shifts), then the columns; pivots mirrored */
+        uint64_t *T = (uint64_t *) calloc((size_t) (m * m * L + 1), sizeof(uint64_t));
+        for (int64_t i = 0; i < nul; i++)
+            for (int64_t j = 0; j < m; j++)
+                memcpy(T + (i * m + j) * L, K + ((nul - 1 - i) * m + (m - 1 - j)) * L, sizeof(uint64_t) * (size_t) L);
+        free(K);
+        K = T;
+        for (int64_t i = 0; i < nul / 2; i++)
+        {
+            int64_t t = sh[i]; sh[i] = sh[nul - 1 - i]; sh[nul - 1 - i] = t;
+            const int64_t a = m - 1 - pivind[i];
+            pivind[i] = m - 1 - pivind[nul - 1 - i];
+            pivind[nul - 1 - i] = a;
+        }
+        if (nul % 2)
+            pivind[nul / 2] = m - 1 - pivind[nul / 2];
+    }
+    if (!left)
+    {
+        uint64_t *T = pm_transpose(K, m, m, L);
+        free(K);
+        K = T;
+    }
+    if (shift)
+        memcpy(shift, sh, sizeof(int64_t) * (size_t) m);
+    free(sh);
+    *ker = K;
+    *klen = L;
+    return nul;
+}

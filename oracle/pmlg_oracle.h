@@ -148,6 +148,18 @@ void orc_multimod_crt(uint64_t *out, const uint64_t *residues, int64_t nb,
 int64_t orc_kernel_zls(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift,
                        const uint64_t *pmat, int64_t m, int64_t n, int64_t plen, uint64_t p,
                        int nthreads);
+/* nmod_poly_mat_kernel_via_approx (kernel.c:146-227): same conventions as
+ * orc_kernel_zls. */
+int64_t orc_kernel_via_approx(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift,
+                              const uint64_t *pmat, int64_t m, int64_t n, int64_t plen, uint64_t p,
+                              int nthreads);
+/* nmod_poly_mat_kernel (kernel.c:26-144), form ORD_WEAK_POPOV, orientation orient
+ * (COL_UPPER 0, COL_LOWER 1, ROW_UPPER 2, ROW_LOWER 3).  pmat: r x c, capacity plen.
+ * Left kernels: *ker is r x r, the basis in its first nullity rows; right kernels:
+ * c x c, the basis in its first nullity columns; other rows / columns zero.  shift
+ * NULL: the default (row or column degrees, zero for zero rows or columns). */
+int64_t orc_kernel(uint64_t **ker, int64_t *klen, int64_t *pivind, int64_t *shift, const uint64_t *pmat,
+                   int64_t r, int64_t c, int64_t plen, uint64_t p, int orient, int nthreads);
 void orc_free(void *ptr);
 
 /* ---- shifted Popov approximant basis ---- */

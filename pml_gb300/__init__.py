@@ -30,6 +30,7 @@ __all__ = [
     "Context", "default_context", "PmlgError", "FORM_AUTO", "FORM_CUDA_CORE", "FORM_INT8_TC", "FORM_F16_TC",
     "nmod_mat_mul_batch", "nmod_poly_mat_multiply", "nmod_poly_mat_mulmid", "nmod_poly_mat_multiply_batch",
     "nmod_poly_mat_pmbasis", "nmod_poly_mat_mbasis", "nmod_poly_mat_popov_pmbasis", "nmod_poly_mat_kernel",
+    "nmod_poly_mat_kernel_oriented", "nmod_poly_mat_kernel_via_approx",
     "nmod_mat_poly_set_trunc_from_poly_mat", "nmod_poly_mat_set_trunc_from_mat_poly",
     "nmod_poly_mat_inv_trunc", "nmod_poly_mat_dixon", "nmod_vec_dot_product", "nmod32_vec_dot_product",
     "nmod32_vec_mdot", "nmod_vec_dot_product_multi", "nmod_multimod_CRT_reduce", "nmod_multimod_CRT_CRT",
@@ -300,6 +301,64 @@ def nmod_poly_mat_set_trunc_from_mat_poly(M, order: int, ctx: Optional[Context] 
     ctx.check(ctx.lib.pmlg_mat_poly_to_poly_mat(ctx.handle, _ptr(out), out.shape[2], _ptr(M), r, c, ln, order,
                                                 _stream_ptr(M)))
     return out
+
+
+ORIENT = {"COL_UPPER": 0, "COL_LOWER": 1, "ROW_UPPER": 2, "ROW_LOWER": 3}
+
+
+def nmod_poly_mat_kernel_oriented(pmat, p: int, orient: str = "ROW_LOWER", shift=None,
+                                  ctx: Optional[Context] = None, cap: Optional[int] = None):
+    """nmod_poly_mat_kernel (kernel.c:26) on the (r, c, len) CUDA tensor pmat, form
+    ORD_WEAK_POPOV: (ker, pivind, shift_out).  Left kernels (ROW_*) give the
+    (nullity, r, length) rows, right kernels (COL_*) the (c, nullity, length)
+    columns.  shift None: the default row / column degrees (shift_out is then None)."""
+    import torch
+    _require_cuda(pmat)
+    ctx = _ctx(ctx, pmat)
+    r, c, plen = pmat.shape
+    o = ORIENT[orient]
+    left = o >= 2
+    m, n = (r, c) if left else (c, r)
+    cap = cap or max(1, (min(m, n) + 1) * max(plen, 1) + 1)
+    while True:
+        sh = None if shift is None else np.ascontiguousarray(shift, dtype=np.int64).copy()
+        piv = np.zeros(max(m, 1), dtype=np.int64)
+        ker = torch.zeros((m, m, cap), dtype=torch.int64, device=pmat.device)
+        ln, nul = C.c_int64(0), C.c_int64(0)
+        st = ctx.lib.pmlg_kernel(ctx.handle, _ptr(ker), cap, C.byref(ln), piv.ctypes.data_as(C.POINTER(C.c_int64)),
+                                 sh.ctypes.data_as(C.POINTER(C.c_int64)) if sh is not None else None, _ptr(pmat),
+                                 r, c, plen, p, 3, o, C.byref(nul), _stream_ptr(pmat))
+        if st == 4 and ln.value > cap:
+            cap = int(ln.value)
+            continue
+        ctx.check(st)
+        k, L = int(nul.value), max(int(ln.value), 1)
+        out = ker[:k, :, :L] if left else ker[:, :k, :L]
+        return out.contiguous(), piv[:k].copy(), (sh[:k].copy() if sh is not None else None)
+
+
+def nmod_poly_mat_kernel_via_approx(pmat, shift, p: int, ctx: Optional[Context] = None, cap: Optional[int] = None):
+    """nmod_poly_mat_kernel_via_approx (kernel.c:146) on a CUDA tensor: (ker, pivind, rdeg)."""
+    import torch
+    _require_cuda(pmat)
+    ctx = _ctx(ctx, pmat)
+    m, n, plen = pmat.shape
+    cap = cap or max(1, (min(m, n) + 2) * max(plen, 1) + 2)
+    while True:
+        sh = np.ascontiguousarray(shift, dtype=np.int64).copy()
+        piv = np.zeros(max(m, 1), dtype=np.int64)
+        ker = torch.zeros((m, m, cap), dtype=torch.int64, device=pmat.device)
+        ln, nul = C.c_int64(0), C.c_int64(0)
+        st = ctx.lib.pmlg_kernel_via_approx(ctx.handle, _ptr(ker), cap, C.byref(ln),
+                                            piv.ctypes.data_as(C.POINTER(C.c_int64)),
+                                            sh.ctypes.data_as(C.POINTER(C.c_int64)), _ptr(pmat), m, n, plen, p,
+                                            C.byref(nul), _stream_ptr(pmat))
+        if st == 4 and ln.value > cap:
+            cap = int(ln.value)
+            continue
+        ctx.check(st)
+        k = int(nul.value)
+        return ker[:k, :, :max(int(ln.value), 1)].contiguous(), piv[:k].copy(), sh[:k].copy()
 
 
 # ---------------------------------------------------------------------------

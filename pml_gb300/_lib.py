@@ -46,6 +46,10 @@ SIGNATURES = {
     "pmlg_pmbasis": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_mbasis": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_pmbasis_host": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
+    "pmlg_kernel_via_approx": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p,
+                                         _vp]),
+    "pmlg_kernel": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, C.c_int, C.c_int,
+                              _i64p, _vp]),
     "pmlg_popov_pmbasis": (C.c_int, [_vp, _vp, _i64, _i64p, _vp, _i64, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_kernel_zls": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p, _vp]),
     "pmlg_kernel_zls_host": (C.c_int, [_vp, _vp, _i64, _i64p, _i64p, _i64p, _vp, _i64, _i64, _i64, _u64, _i64p,

@@ -469,3 +469,277 @@ extern "C" PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64
     if (s == PMLG_ECUDA) set_error(ctx, "host-buffer kernel basis: a copy or an allocation failed");
     return s;
 }
+
+// ---------------------------------------------------------------------------
+// nmod_poly_mat_kernel_via_approx (kernel.c:146-227) and the orientation
+// interface nmod_poly_mat_kernel (kernel.c:26-144)
+// ---------------------------------------------------------------------------
+
+namespace pmlg {
+
+namespace {
+
+// out entry k <- in entry src[k] (zero when src[k] < 0), out capacity ocap, in capacity icap
+__global__ void entry_gather_kernel(uint64_t *__restrict__ out, int64_t ocap, const uint64_t *__restrict__ in,
+                                    int64_t icap, const int *__restrict__ src)
+{
+    const int s = src[blockIdx.x];
+    uint64_t *o = out + (int64_t)blockIdx.x * ocap;
+    for (int64_t d = threadIdx.x; d < ocap; d += blockDim.x)
+        o[d] = (s >= 0 && d < icap) ? in[(int64_t)s * icap + d] : 0ull;
+}
+
+int gather_entries(pmlg_ctx *ctx, uint64_t *out, int64_t ocap, const uint64_t *in, int64_t icap,
+                   const std::vector<int> &src, cudaStream_t st)
+{
+    const int64_t ne = (int64_t)src.size();
+    if (ne == 0) return PMLG_OK;
+    int *d_src = nullptr;
+    PMLG_CUDA_TRY(cudaMallocAsync((void **)&d_src, (size_t)ne * sizeof(int), st));
+    cudaError_t e = cudaMemcpyAsync(d_src, src.data(), (size_t)ne * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+        prof_begin(ctx, "entry_gather", st);
+        entry_gather_kernel<<<(unsigned)ne, 128, 0, st>>>(out, ocap, in, icap, d_src);
+        prof_end(ctx, st);
+        count_launch(ctx);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(d_src, st);
+    // the index map is a host vector: it must outlive the copy
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_error(ctx, "entry gather: %s", cudaGetErrorString(e));
+        return PMLG_ECUDA;
+    }
+    return PMLG_OK;
+}
+
+int64_t rank_mod_h(std::vector<uint64_t> a, int64_t r, int64_t c, uint64_t p)
+{
+    int64_t rank = 0;
+    for (int64_t col = 0; col < c && rank < r; col++) {
+        int64_t piv = -1;
+        for (int64_t i = rank; i < r; i++)
+            if (a[(size_t)(i * c + col)] % p) { piv = i; break; }
+        if (piv < 0) continue;
+        for (int64_t j = 0; j < c; j++) std::swap(a[(size_t)(piv * c + j)], a[(size_t)(rank * c + j)]);
+        uint64_t inv = 1, b = a[(size_t)(rank * c + col)] % p, e = p - 2;
+        while (e) {
+            if (e & 1) inv = (uint64_t)((unsigned __int128)inv * b % p);
+            b = (uint64_t)((unsigned __int128)b * b % p);
+            e >>= 1;
+        }
+        for (int64_t i = rank + 1; i < r; i++) {
+            const uint64_t f = (uint64_t)((unsigned __int128)(a[(size_t)(i * c + col)] % p) * inv % p);
+            if (!f) continue;
+            for (int64_t j = col; j < c; j++) {
+                const uint64_t t = (uint64_t)((unsigned __int128)f * (a[(size_t)(rank * c + j)] % p) % p);
+                const uint64_t x = a[(size_t)(i * c + j)] % p;
+                a[(size_t)(i * c + j)] = x >= t ? x - t : x + p - t;
+            }
+        }
+        rank++;
+    }
+    return rank;
+}
+
+int check_kernel_args(pmlg_ctx *ctx, int64_t m, uint64_t p)
+{
+    if (m > 64) {
+        set_error(ctx, "kernel bases support m <= 64 (the approximant bases' limit)");
+        return PMLG_EUNSUP;
+    }
+    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
+        set_error(ctx, "kernel bases need a prime p < 2^30");
+        return PMLG_EBADMOD;
+    }
+    return PMLG_OK;
+}
+
+}  // namespace
+
+}  // namespace pmlg
+
+extern "C" PMLG_API int pmlg_kernel_via_approx(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len,
+                                               int64_t *pivind, int64_t *shift, const uint64_t *pmat, int64_t m,
+                                               int64_t n, int64_t plen, uint64_t p, int64_t *nullity, void *stream)
+{
+    if (!ctx || m < 0 || n < 0 || plen < 0 || ker_cap < 1 || !nullity || !ker_len) return PMLG_EINVAL;
+    if (m > 0 && (!ker || !pivind || !shift)) return PMLG_EINVAL;
+    if (m > 0 && n > 0 && plen > 0 && !pmat) return PMLG_EINVAL;
+    PMLG_TRY(check_kernel_args(ctx, m, p));
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    *nullity = 0;
+    *ker_len = 1;
+    if (m == 0) return PMLG_OK;
+    const int64_t ne = m * n, cap0 = plen > 0 ? plen : 1;
+    int *d_len = nullptr;
+    PMLG_CUDA_TRY(cudaMallocAsync((void **)&d_len, (size_t)(ne > 0 ? ne : 1) * sizeof(int) + 64, st));
+    std::vector<int> len;
+    int s = (ne > 0 && plen > 0) ? entry_lengths(ctx, pmat, ne, plen, d_len, len, st) : PMLG_OK;
+    cudaFreeAsync(d_len, st);
+    PMLG_TRY(s);
+    int64_t L = 0;
+    for (int v : len) L = v > L ? v : L;
+    const int64_t d = L - 1;
+    const size_t kbytes = (size_t)(m * m * ker_cap) * 8;
+    if (d == -1) {   // zero matrix: the identity
+        PMLG_CUDA_TRY(cudaMemsetAsync(ker, 0, kbytes, st));
+        const uint64_t one = 1;
+        for (int64_t i = 0; i < m; i++) {
+            PMLG_CUDA_TRY(cudaMemcpyAsync(ker + (i * m + i) * ker_cap, &one, 8, cudaMemcpyHostToDevice, st));
+            pivind[i] = i;
+        }
+        PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+        *nullity = m;
+        return PMLG_OK;
+    }
+    if (m == 1) return PMLG_OK;
+    if (m <= n) {
+        // full row rank of the constant coefficient: empty kernel (:171-184)
+        std::vector<uint64_t> c0((size_t)ne);
+        PMLG_CUDA_TRY(cudaMemcpy2DAsync(c0.data(), 8, pmat, (size_t)cap0 * 8, 8, (size_t)ne, cudaMemcpyDeviceToHost, st));
+        PMLG_CUDA_TRY(cudaStreamSynchronize(st));
+        if (rank_mod_h(c0, m, n, p) == m) return PMLG_OK;
+    }
+    int64_t mn = shift[0], amp = shift[0];
+    std::vector<int64_t> rdeg((size_t)m);
+    for (int64_t i = 0; i < m; i++) {
+        rdeg[(size_t)i] = shift[i];
+        if (shift[i] < mn) mn = shift[i];
+        else if (shift[i] > amp) amp = shift[i];
+    }
+    amp -= mn;
+    const int64_t order = (m < n ? m : n) * d + amp + d + 1, cap = order + 1;
+    uint64_t *K = nullptr;
+    PMLG_CUDA_TRY(cudaMallocAsync((void **)&K, (size_t)(m * m * cap) * 8 + 8, st));
+    int64_t alen = 0;
+    s = pmbasis_device(ctx, K, cap, rdeg.data(), pmat, m, n, cap0, order, p, &alen, st);
+    // rows that are kernel rows, moved to the front by swaps (:209-224)
+    std::vector<int> src((size_t)(m * m), -1);
+    int64_t nul = 0;
+    if (s == PMLG_OK) {
+        std::vector<int64_t> rowof((size_t)m);
+        for (int64_t i = 0; i < m; i++) rowof[(size_t)i] = i;
+        for (int64_t i = 0; i < m; i++) {
+            if (rdeg[(size_t)i] - shift[i] + amp < order - d) {
+                shift[nul] = rdeg[(size_t)i];
+                pivind[nul] = i;
+                std::swap(rowof[(size_t)nul], rowof[(size_t)i]);
+                nul++;
+            }
+        }
+        for (int64_t i = 0; i < nul; i++)
+            for (int64_t j = 0; j < m; j++) src[(size_t)(i * m + j)] = (int)(rowof[(size_t)i] * m + j);
+        // the length of the kernel rows
+        int *d2 = nullptr;
+        std::vector<int> klen;
+        if (cudaMallocAsync((void **)&d2, (size_t)(m * m) * sizeof(int) + 64, st) != cudaSuccess) s = PMLG_ECUDA;
+        if (s == PMLG_OK) s = entry_lengths(ctx, K, m * m, cap, d2, klen, st);
+        if (d2) cudaFreeAsync(d2, st);
+        int64_t KL = 0;
+        if (s == PMLG_OK)
+            for (int64_t i = 0; i < nul; i++)
+                for (int64_t j = 0; j < m; j++) KL = std::max<int64_t>(KL, klen[(size_t)(rowof[(size_t)i] * m + j)]);
+        *ker_len = KL > 0 ? KL : 1;
+        *nullity = nul;
+        if (s == PMLG_OK && *ker_len > ker_cap) {
+            set_error(ctx, "the kernel basis has length %lld, above the capacity %lld", (long long)*ker_len,
+                      (long long)ker_cap);
+            s = PMLG_ELEN;
+        }
+        if (s == PMLG_OK) s = gather_entries(ctx, ker, ker_cap, K, cap, src, st);
+    }
+    cudaFreeAsync(K, st);
+    if (s == PMLG_OK) s = device_status(ctx, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == PMLG_OK) s = PMLG_ECUDA;
+    return s;
+}
+
+extern "C" PMLG_API int pmlg_kernel(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap, int64_t *ker_len, int64_t *pivind,
+                                    int64_t *shift, const uint64_t *pmat, int64_t r, int64_t c, int64_t plen,
+                                    uint64_t p, int form, int orient, int64_t *nullity, void *stream)
+{
+    if (!ctx || r < 0 || c < 0 || plen < 0 || ker_cap < 1 || !nullity || !ker_len) return PMLG_EINVAL;
+    if (orient < PMLG_COL_UPPER || orient > PMLG_ROW_LOWER) return PMLG_EINVAL;
+    if (form > PMLG_ORD_WEAK_POPOV) {
+        set_error(ctx, "kernel bases: forms beyond ordered weak Popov are not implemented (as in kernel.c:34)");
+        return PMLG_EUNSUP;
+    }
+    const bool left = orient == PMLG_ROW_UPPER || orient == PMLG_ROW_LOWER;
+    const bool rev = orient == PMLG_ROW_UPPER || orient == PMLG_COL_LOWER;
+    const int64_t m = left ? r : c, n = left ? c : r;
+    if (m > 0 && (!ker || !pivind)) return PMLG_EINVAL;
+    if (r > 0 && c > 0 && plen > 0 && !pmat) return PMLG_EINVAL;
+    PMLG_TRY(check_kernel_args(ctx, m, p));
+    cudaStream_t st = (cudaStream_t)stream;
+    PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
+    *nullity = 0;
+    *ker_len = 1;
+    if (m == 0) return PMLG_OK;
+    const int64_t ne = r * c, cap0 = plen > 0 ? plen : 1;
+    // the shift: the caller's, or the row / column degrees (zero for zero rows / columns)
+    std::vector<int64_t> sh((size_t)m, 0);
+    if (shift) {
+        for (int64_t i = 0; i < m; i++) sh[(size_t)i] = shift[i];
+    } else if (ne > 0 && plen > 0) {
+        int *d_len = nullptr;
+        std::vector<int> len;
+        PMLG_CUDA_TRY(cudaMallocAsync((void **)&d_len, (size_t)ne * sizeof(int) + 64, st));
+        const int s0 = entry_lengths(ctx, pmat, ne, plen, d_len, len, st);
+        cudaFreeAsync(d_len, st);
+        PMLG_TRY(s0);
+        for (int64_t i = 0; i < m; i++)
+            for (int64_t j = 0; j < n; j++) {
+                const int l = left ? len[(size_t)(i * c + j)] : len[(size_t)(j * c + i)];
+                sh[(size_t)i] = std::max<int64_t>(sh[(size_t)i], l > 0 ? l - 1 : 0);
+            }
+    }
+    // the ROW_LOWER problem: transposed for right kernels, rows reversed for ROW_UPPER / COL_LOWER
+    std::vector<int> src((size_t)(m * n));
+    for (int64_t i = 0; i < m; i++) {
+        const int64_t ii = rev ? m - 1 - i : i;
+        for (int64_t j = 0; j < n; j++) src[(size_t)(i * n + j)] = (int)(left ? ii * c + j : j * c + ii);
+    }
+    if (rev) std::reverse(sh.begin(), sh.end());
+    uint64_t *M = nullptr, *K = nullptr;
+    PMLG_CUDA_TRY(cudaMallocAsync((void **)&M, (size_t)(m * n * cap0) * 8 + 8, st));
+    int s = PMLG_OK;
+    if (cudaMallocAsync((void **)&K, (size_t)(m * m * ker_cap) * 8 + 8, st) != cudaSuccess) s = PMLG_ECUDA;
+    if (s == PMLG_OK && ne > 0) {
+        if (plen > 0) s = gather_entries(ctx, M, cap0, pmat, plen, src, st);
+        else if (cudaMemsetAsync(M, 0, (size_t)(m * n * cap0) * 8, st) != cudaSuccess) s = PMLG_ECUDA;
+    }
+    int64_t nul = 0;
+    if (s == PMLG_OK)
+        s = pmlg_kernel_zls(ctx, K, ker_cap, ker_len, pivind, sh.data(), M, m, n, ne > 0 ? cap0 : 0, p, &nul, stream);
+    if (s == PMLG_OK) {
+        if (rev && nul > 0) {
+            // kernel rows reversed (and their shifts), columns reversed, pivots mirrored (:91-103)
+            std::reverse(sh.begin(), sh.begin() + nul);
+            for (int64_t i = 0; i < nul / 2; i++) {
+                const int64_t t = m - 1 - pivind[i];
+                pivind[i] = m - 1 - pivind[nul - 1 - i];
+                pivind[nul - 1 - i] = t;
+            }
+            if (nul % 2) pivind[nul / 2] = m - 1 - pivind[nul / 2];
+        }
+        // final entry (a, b): rows a < nullity of the (reversed) kernel, transposed for right kernels
+        std::vector<int> fsrc((size_t)(m * m), -1);
+        for (int64_t a = 0; a < m; a++)
+            for (int64_t b = 0; b < m; b++) {
+                const int64_t i = left ? a : b, j = left ? b : a;   // kernel row i, column j
+                if (i >= nul) continue;
+                fsrc[(size_t)(a * m + b)] = (int)(rev ? (nul - 1 - i) * m + (m - 1 - j) : i * m + j);
+            }
+        s = gather_entries(ctx, ker, ker_cap, K, ker_cap, fsrc, st);
+        *nullity = nul;
+        if (shift)
+            for (int64_t i = 0; i < m; i++) shift[i] = sh[(size_t)i];
+    }
+    cudaFreeAsync(M, st);
+    if (K) cudaFreeAsync(K, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess && s == PMLG_OK) s = PMLG_ECUDA;
+    return s;
+}

@@ -75,3 +75,45 @@ def test_kernel_host_path(ctx):
     kh, ph, rh = pml_gb300.nmod_poly_mat_kernel(F, list(range(10)), p, ctx=ctx)
     kd, pd, rd = _gpu_kernel(ctx, F, list(range(10)), p)
     assert np.array_equal(kh, kd) and list(ph) == pd and list(rh) == rd
+
+
+@pytest.mark.parametrize("dims", [(6, 2, 4), (8, 3, 3), (7, 3, 5), (3, 6, 2), (5, 5, 2), (2, 7, 3), (40, 12, 6),
+                                  (12, 40, 5)])
+@pytest.mark.parametrize("orient", ["ROW_LOWER", "ROW_UPPER", "COL_UPPER", "COL_LOWER"])
+def test_kernel_orientations(ctx, dims, orient):
+    """pmlg_kernel in every orientation, default shift and an explicit one, against the
+    oracle's nmod_poly_mat_kernel (kernel.c:26-144) bit for bit."""
+    import pml_gb300
+    r, c, d = dims
+    p = P998
+    F = oracle.rand_poly_mat(r, c, d + 1, p, r * c + d)
+    m = r if orient.startswith("ROW") else c
+    for shift in (None, [(5 * i) % 3 for i in range(m)]):
+        ker, piv, sh = pml_gb300.nmod_poly_mat_kernel_oriented(to_dev(F), p, orient, shift, ctx=ctx)
+        rker, rpiv, rsh, nul = oracle.kernel(F, shift, p, orient)
+        ker = to_host(ker)
+        assert list(piv) == list(rpiv)
+        if shift is not None:
+            assert list(sh) == list(rsh)
+        L = max(ker.shape[2], rker.shape[2])
+        pad = lambda a: np.concatenate([a, np.zeros(a.shape[:2] + (L - a.shape[2],), dtype=np.uint64)], axis=2)
+        assert np.array_equal(pad(ker), pad(rker))
+
+
+@pytest.mark.parametrize("dims", [(6, 2, 4), (8, 3, 3), (5, 5, 2), (1, 3, 4), (16, 4, 6)])
+def test_kernel_via_approx(ctx, dims):
+    import pml_gb300
+    m, n, d = dims
+    p = P998
+    F = oracle.rand_poly_mat(m, n, d + 1, p, 7 * m + n)
+    for shift in ([0] * m, list(range(m))):
+        ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel_via_approx(to_dev(F), shift, p, ctx=ctx)
+        rker, rpiv, rrdeg, nul = oracle.kernel_via_approx(F, shift, p)
+        ker = to_host(ker)
+        assert ker.shape[0] == nul and list(piv) == list(rpiv) and list(rdeg) == list(rrdeg)
+        L = max(ker.shape[2], rker.shape[2])
+        pad = lambda a: np.concatenate([a, np.zeros(a.shape[:2] + (L - a.shape[2],), dtype=np.uint64)], axis=2)
+        assert np.array_equal(pad(ker), pad(rker))
+    Z = np.zeros((4, 2, 3), dtype=np.uint64)
+    ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel_via_approx(to_dev(Z), [0] * 4, p, ctx=ctx)
+    assert ker.shape[0] == 4 and list(piv) == [0, 1, 2, 3]

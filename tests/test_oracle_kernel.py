@@ -55,3 +55,50 @@ def test_oracle_kernel_degenerate():
     check_kernel(oracle.rand_poly_mat(1, 3, 4, P, 10), [0], P)
     check_kernel(oracle.rand_poly_mat(5, 1, 4, P, 11), [0] * 5, P)
     check_kernel(oracle.rand_poly_mat(5, 1, 4, 7, 12), [0] * 5, 7)
+
+
+def _pivots_upper(ker, shift):
+    """s-row degree and s-pivot (the leftmost column reaching it: ROW_UPPER)."""
+    rows, cols, L = ker.shape
+    out = []
+    for i in range(rows):
+        best, bj = None, -1
+        for j in range(cols):
+            nz = np.nonzero(ker[i, j])[0]
+            if len(nz) == 0:
+                continue
+            v = int(nz[-1]) + int(shift[j])
+            if best is None or v > best:
+                best, bj = v, j
+        out.append(bj)
+    return out
+
+
+@pytest.mark.parametrize("dims", [(6, 2, 4), (8, 3, 3), (7, 3, 5), (3, 6, 2), (5, 5, 2), (2, 7, 3)])
+def test_oracle_kernel_orientations(dims):
+    """nmod_poly_mat_kernel (kernel.c:26-144): left kernels K F = 0 with pivots on the
+    right (ROW_LOWER) or the left (ROW_UPPER), right kernels F K = 0 through the
+    transpose, and kernel_via_approx on the same inputs."""
+    r, c, d = dims
+    p = P
+    F = oracle.rand_poly_mat(r, c, d + 1, p, r * c + d)
+    for orient in ("ROW_LOWER", "ROW_UPPER"):
+        ker, piv, _, nul = oracle.kernel(F, None, p, orient)
+        assert nul == r - _rank_at_point(F, p)
+        if nul:
+            assert not oracle.poly_mat_mul(ker, F, p).any()
+            rdeg0 = [max([int(np.nonzero(F[i, j])[0][-1]) for j in range(c) if F[i, j].any()] or [0])
+                     for i in range(r)]
+            want = oracle.row_degrees_and_pivots(ker, rdeg0)[1] if orient == "ROW_LOWER" else _pivots_upper(ker, rdeg0)
+            assert list(piv) == list(want)
+    for orient in ("COL_UPPER", "COL_LOWER"):
+        ker, piv, _, nul = oracle.kernel(F, None, p, orient)
+        assert nul == c - _rank_at_point(F, p)
+        if nul:
+            assert not oracle.poly_mat_mul(F, ker, p).any()
+    ker, piv, rdeg, nul = oracle.kernel_via_approx(F, [0] * r, p)
+    assert nul == r - _rank_at_point(F, p)
+    if nul:
+        assert not oracle.poly_mat_mul(ker, F, p).any()
+        rd, pv = oracle.row_degrees_and_pivots(ker, [0] * r)
+        assert list(pv) == list(piv) and list(rd) == list(rdeg)
