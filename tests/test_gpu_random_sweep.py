@@ -1,0 +1,86 @@
+"""A fixed-seed randomized differential sweep of the GPU library against the
+oracle: products (every form, moduli from 20 to 62 bits, device and host
+buffers), middle products, pmbasis and shift-Popov bases (random shifts, zero
+rows), kernel bases in every orientation, and batches of products.  Bounded to
+a fixed number of cases so it runs in seconds."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import oracle
+from conftest import P998, to_dev, to_host
+
+pytestmark = pytest.mark.gpu
+
+CASES = 140
+
+
+def _pad(a, L):
+    return np.concatenate([a, np.zeros(a.shape[:2] + (L - a.shape[2],), dtype=np.uint64)], axis=2)
+
+
+def test_random_sweep(ctx):
+    import pml_gb300
+    rng = np.random.default_rng(2026)
+    kinds = ["mul", "mulhost", "mulmid", "pmbasis", "popov", "kernel", "batch"]
+    for case in range(CASES):
+        kind = kinds[case % len(kinds)]
+        pbits = int(rng.integers(20, 63)) if kind in ("mul", "mulhost", "mulmid", "batch") else int(rng.integers(20, 31))
+        p = P998 if rng.random() < 0.3 else oracle.rand_prime(pbits, int(rng.integers(1, 10 ** 6)))
+        seed = int(rng.integers(1, 10 ** 9))
+        info = (case, kind, p, seed)
+        if kind in ("mul", "mulhost", "mulmid"):
+            r, k, c = (int(x) for x in rng.integers(1, 20, size=3))
+            l1, l2 = (int(x) for x in rng.integers(1, 200, size=2))
+            A = oracle.rand_poly_mat(r, k, l1, p, seed)
+            B = oracle.rand_poly_mat(k, c, l2, p, seed + 1)
+            ctx.set_form(int(rng.integers(0, 4)))
+            if kind == "mul":
+                out = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), p, ctx=ctx))
+                ref = oracle.poly_mat_mul(A, B, p, nthreads=8)
+            elif kind == "mulhost":
+                out = pml_gb300.nmod_poly_mat_multiply(A, B, p, ctx=ctx)
+                ref = oracle.poly_mat_mul(A, B, p, nthreads=8)
+            else:
+                nlo = int(rng.integers(0, l1 + l2))
+                nhi = nlo + int(rng.integers(1, l1 + l2))
+                out = to_host(pml_gb300.nmod_poly_mat_mulmid(to_dev(A), to_dev(B), nlo, nhi, p, ctx=ctx))
+                ref = oracle.poly_mat_mulmid(A, B, nlo, nhi, p, nthreads=8)[0]
+            ctx.set_form(0)
+            assert out.shape == ref.shape and np.array_equal(out, ref), info
+        elif kind in ("pmbasis", "popov"):
+            m = int(rng.integers(1, 65))
+            n = int(rng.integers(1, min(m, 32) + 1))
+            order = int(rng.integers(1, 120))
+            F = oracle.rand_poly_mat(m, n, int(rng.integers(1, order + 5)), p, seed)
+            if rng.random() < 0.3:
+                F[int(rng.integers(0, m))] = 0
+            sh = [int(x) for x in rng.integers(0, order, size=m)] if rng.random() < 0.5 else [0] * m
+            fn = pml_gb300.nmod_poly_mat_pmbasis if kind == "pmbasis" else pml_gb300.nmod_poly_mat_popov_pmbasis
+            ofn = oracle.pmbasis if kind == "pmbasis" else oracle.popov_pmbasis
+            ab, s2 = fn(to_dev(F), order, sh, p, ctx=ctx)
+            ref, rs = ofn(F, order, sh, p, nthreads=8)
+            ab = to_host(ab)
+            L = max(ab.shape[2], ref.shape[2])
+            assert list(s2) == list(rs) and np.array_equal(_pad(ab, L), _pad(ref, L)), info
+        elif kind == "kernel":
+            r, c = (int(x) for x in rng.integers(1, 33, size=2))
+            F = oracle.rand_poly_mat(r, c, int(rng.integers(1, 8)), p, seed)
+            orient = ["ROW_LOWER", "ROW_UPPER", "COL_UPPER", "COL_LOWER"][case % 4]
+            ker, piv, _ = pml_gb300.nmod_poly_mat_kernel_oriented(to_dev(F), p, orient, None, ctx=ctx)
+            rk, rp, _, nul = oracle.kernel(F, None, p, orient)
+            ker = to_host(ker)
+            L = max(ker.shape[2], rk.shape[2])
+            assert list(piv) == list(rp) and np.array_equal(_pad(ker, L), _pad(rk, L)), info
+        else:
+            jobs, refs = [], []
+            for j in range(int(rng.integers(1, 8))):
+                m = int(rng.integers(1, 20))
+                ln = int(rng.integers(1, 200))
+                A = oracle.rand_poly_mat(m, m, ln, p, seed + 2 * j)
+                B = oracle.rand_poly_mat(m, m, ln, p, seed + 2 * j + 1)
+                jobs.append((to_dev(A), to_dev(B), p))
+                refs.append(oracle.poly_mat_mul(A, B, p, nthreads=8))
+            outs = pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx)
+            assert all(np.array_equal(to_host(o), r) for o, r in zip(outs, refs)), info
