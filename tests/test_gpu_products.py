@@ -114,6 +114,21 @@ def test_products_random(fctx, dims, p):
     assert np.array_equal(_mul(fctx, A, B, p), oracle.poly_mat_mul(A, B, p, nthreads=8))
 
 
+@pytest.mark.parametrize("dims", [(3, 4, 2, 2500, 1800), (2, 3, 2, 3000, 100), (2, 2, 1, 8000, 5000),
+                                  (1, 1, 1, 2048, 2048)])
+@pytest.mark.parametrize("p", [P998, 2305843009213693951, 18446744073709551557])
+def test_products_large_transforms(fctx, dims, p):
+    """Transform lengths 4096 to 16384, where the forward transforms of operands of at
+    most N/2 coefficients run persistently with their next coefficients staged in
+    shared memory (as 32-bit words for p = 998244353, whole 64-bit words when the
+    coefficients need reduction modulo each CRT prime), and longer operands take the
+    one-transform-per-CTA kernel: bit-exact against the oracle."""
+    r, k, c, l1, l2 = dims
+    A = oracle.rand_poly_mat(r, k, l1, p, 31)
+    B = oracle.rand_poly_mat(k, c, l2, p, 32)
+    assert np.array_equal(_mul(fctx, A, B, p), oracle.poly_mat_mul(A, B, p, nthreads=8))
+
+
 def test_products_config1_plain(fctx):
     """16x16 . 16x16, degree < 256, p = 998244353 (the CPU-runnable case)."""
     p = P998
