@@ -7,8 +7,12 @@
 // exactly when the basis' bottom-right block is the identity, and the inverse is its
 // bottom-left block.  Dixon lifting then produces one x-adic digit of X per step with
 // the library's middle product and product, and one fused kernel forms the next
-// residue (B - A S) div x^order.  Every matrix stays in device memory.
+// residue (B - A S) div x^order.  The two left operands that every step shares, the
+// truncated inverse and A, are transformed once: their evaluations are kept across
+// the steps, as _nmod_poly_mat_mul_geometric_precomp keeps them
+// (mul_geometric.c:32-119).  Every matrix stays in device memory.
 #include "pmlg_internal.cuh"
+#include "ntt.cuh"
 #include "polymat.cuh"
 
 #include <vector>
@@ -187,13 +191,31 @@ extern "C" PMLG_API int pmlg_dixon(pmlg_ctx *ctx, uint64_t *X, int64_t xcap, con
         uint64_t *AS = mem.get(ne * tl);
         if (!BB || !NBbuf || !Sl || !AS) return PMLG_ENOMEM;
         if (blen > 0) PMLG_CUDA_TRY(cudaMemcpyAsync(BB, B, (size_t)(ne * blen) * 8, cudaMemcpyDeviceToDevice, st));
+        // evaluation caches sized for the largest transform and prime count of each product
+        // (the middle product needs at most 2 order - 1 points, the product alen + order - 1)
+        EvalCache cC, cA;
+        {
+            CrtPlan pl;
+            const int lgC = lg_for(2 * order - 1), lgA = lg_for((alen > 0 ? alen : 1) + order - 1);
+            if (lgC <= kMaxLgN && make_plan(ctx, p, lgC, n, order, &pl) == PMLG_OK) {
+                cC.words = (size_t)pl.t * ((size_t)1 << lgC) * (size_t)(n * n);
+                cC.ea = (uint32_t *)mem.get((int64_t)(cC.words + 1) / 2);
+                if (!cC.ea) cC.words = 0;
+            }
+            if (alen > 0 && lgA <= kMaxLgN &&
+                make_plan(ctx, p, lgA, n, alen < order ? alen : order, &pl) == PMLG_OK) {
+                cA.words = (size_t)pl.t * ((size_t)1 << lgA) * (size_t)(n * n);
+                cA.ea = (uint32_t *)mem.get((int64_t)(cA.words + 1) / 2);
+                if (!cA.ea) cA.words = 0;
+            }
+        }
         for (int64_t l = 0; l * order < sigma; l++) {
             // S = C * BB mod x^order; X += x^(l order) S
-            PMLG_TRY(poly_mat_mulmid_device(ctx, Sl, Cinv, BB, n, n, m, ccap, bcap, 0, order, p, st));
+            PMLG_TRY(poly_mat_mulmid_device(ctx, Sl, Cinv, BB, n, n, m, ccap, bcap, 0, order, p, st, &cC));
             PMLG_CUDA_TRY(cudaMemcpy2DAsync(X + l * order, (size_t)xcap * 8, Sl, (size_t)order * 8, (size_t)order * 8,
                                             (size_t)ne, cudaMemcpyDeviceToDevice, st));
             // BB = (BB - A S) div x^order
-            if (alen > 0) PMLG_TRY(poly_mat_mul_device(ctx, AS, A, Sl, n, n, m, alen, order, p, st));
+            if (alen > 0) PMLG_TRY(poly_mat_mul_device(ctx, AS, A, Sl, n, n, m, alen, order, p, st, &cA));
             else PMLG_CUDA_TRY(cudaMemsetAsync(AS, 0, (size_t)(ne * tl) * 8, st));
             const int64_t hi = bcap > tl ? bcap : tl;
             const int64_t ncap = hi - order > 0 ? hi - order : 1;

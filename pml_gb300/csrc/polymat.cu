@@ -129,11 +129,33 @@ static int product_inverse(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &pl
 }
 
 int product_run(pmlg_ctx *ctx, const ProductJob &j, const CrtPlan &plan, void *scratch, int form,
-                cudaStream_t st)
+                cudaStream_t st, EvalCache *ca)
 {
     ProductBufs b;
     PMLG_TRY(product_bufs(ctx, j, plan, scratch, b));
-    PMLG_TRY(product_forward(ctx, j, plan, b, 0, 0, j.r * j.k, st));
+    const size_t need = (size_t)plan.t * ((size_t)1 << j.lg) * (size_t)(j.r * j.k);
+    if (ca && ca->ea && need <= ca->words) {
+        bool same = ca->valid && ca->lg == j.lg && ca->t == plan.t && ca->a == j.A && ca->r == j.r && ca->k == j.k && ca->lda == j.lda &&
+                    ca->a_off == j.a_off && ca->a_len == j.a_len;
+        for (int i = 0; same && i < plan.t; i++) same = ca->q[i] == plan.q[i];
+        b.EA = ca->ea;
+        if (!same) {
+            ca->valid = false;
+            PMLG_TRY(product_forward(ctx, j, plan, b, 0, 0, j.r * j.k, st));
+            ca->valid = true;
+            ca->lg = j.lg;
+            ca->t = plan.t;
+            for (int i = 0; i < plan.t; i++) ca->q[i] = plan.q[i];
+            ca->a = j.A;
+            ca->r = j.r;
+            ca->k = j.k;
+            ca->lda = j.lda;
+            ca->a_off = j.a_off;
+            ca->a_len = j.a_len;
+        }
+    } else {
+        PMLG_TRY(product_forward(ctx, j, plan, b, 0, 0, j.r * j.k, st));
+    }
     PMLG_TRY(product_forward(ctx, j, plan, b, 1, 0, j.k * j.c, st));
     PMLG_TRY(product_pointwise(ctx, j, plan, b, 0, j.r, form, st));
     return product_inverse(ctx, j, plan, b, 0, j.r * j.c, st);
@@ -216,13 +238,13 @@ static bool overlaps(const void *a, size_t na, const void *b, size_t nb)
 // entry points
 // ---------------------------------------------------------------------------
 
-static int run_job_alloc(pmlg_ctx *ctx, const ProductJob &j, cudaStream_t st)
+static int run_job_alloc(pmlg_ctx *ctx, const ProductJob &j, cudaStream_t st, EvalCache *ca = nullptr)
 {
     CrtPlan plan;
     const int64_t minlen = j.a_len < j.b_len ? j.a_len : j.b_len;
     PMLG_TRY(make_plan(ctx, j.p, j.lg, j.k, minlen, &plan));
     PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan)));
-    return product_run(ctx, j, plan, ctx->ws.ptr, ctx->form, st);
+    return product_run(ctx, j, plan, ctx->ws.ptr, ctx->form, st, ca);
 }
 
 // the job of a full product C = A * B with coefficient-contiguous entries
@@ -253,7 +275,8 @@ static int ensure_side_streams(pmlg_ctx *ctx, int nstreams)
 }
 
 int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uint64_t *B, int64_t r,
-                        int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p, cudaStream_t st)
+                        int64_t k, int64_t c, int64_t len1, int64_t len2, uint64_t p, cudaStream_t st,
+                        EvalCache *ca)
 {
     const int64_t clen = (len1 > 0 && len2 > 0) ? len1 + len2 - 1 : 0;
     if (r == 0 || c == 0 || clen == 0) return PMLG_OK;
@@ -267,12 +290,12 @@ int poly_mat_mul_device(pmlg_ctx *ctx, uint64_t *C, const uint64_t *A, const uin
         set_error(ctx, "product length %lld needs a transform beyond 2^%d", (long long)clen, kMaxLgN);
         return PMLG_ELEN;
     }
-    return run_job_alloc(ctx, j, st);
+    return run_job_alloc(ctx, j, st, ca);
 }
 
 int poly_mat_mulmid_device(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, const uint64_t *B,
                            int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2, int64_t nlo,
-                           int64_t nhi, uint64_t p, cudaStream_t st)
+                           int64_t nhi, uint64_t p, cudaStream_t st, EvalCache *ca)
 {
     const int64_t cap = nhi - nlo;
     if (cap <= 0 || r == 0 || c == 0) return PMLG_OK;
@@ -291,7 +314,7 @@ int poly_mat_mulmid_device(pmlg_ctx *ctx, uint64_t *res, const uint64_t *A, cons
         set_error(ctx, "middle product needs a transform beyond 2^%d", kMaxLgN);
         return PMLG_ELEN;
     }
-    return run_job_alloc(ctx, j, st);
+    return run_job_alloc(ctx, j, st, ca);
 }
 
 static int check_common(pmlg_ctx *ctx, const void *C, const void *A, const void *B, int64_t r, int64_t k,

@@ -35,6 +35,24 @@ def test_dixon(ctx, n, m, alen, blen, order, sigma):
     assert ok and rok and np.array_equal(to_host(X), rX)
 
 
+@pytest.mark.parametrize("p", [1000003, 1073741789, 998244353])
+@pytest.mark.parametrize("n,m,alen,blen,order,sigma", [(4, 3, 5, 7, 16, 100), (6, 2, 9, 40, 12, 130),
+                                                        (3, 5, 2, 3, 1, 20)])
+def test_dixon_primes_and_lengths(ctx, p, n, m, alen, blen, order, sigma):
+    """Moduli that take one NTT prime or CRT over several, a right-hand side longer
+    than the digits (the residue shrinks over the first steps, so the middle product's
+    transform size changes and the kept evaluations of the inverse are made again), and
+    digits of one coefficient: bit-exact against the oracle."""
+    import pml_gb300
+    A = oracle.rand_poly_mat(n, n, alen, p, 7 * n + alen)
+    B = oracle.rand_poly_mat(n, m, blen, p, 11 * m + blen)
+    X, ok = pml_gb300.nmod_poly_mat_dixon(to_dev(A), to_dev(B), order, sigma, p, ctx=ctx)
+    rX, rok = oracle.dixon(A, B, order, sigma, p, nthreads=8)
+    assert ok == rok
+    if rok:
+        assert np.array_equal(to_host(X), rX)
+
+
 def test_singular_and_property(ctx):
     import pml_gb300
     p = P998
