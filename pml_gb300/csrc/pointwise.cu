@@ -609,10 +609,16 @@ pw_f16_kernel(PwArgs a)
             for (int pp = 0; pp < 2; pp++, p++) {
                 uint32_t *row = Cst + (pp * 2 + hi) * F16_CST_WORDS + i * F16_CST_LD;
                 for (int h = 0; h < 2; h++) {
+                    // Packed blocks (2^lmt <= 32): the outputs of region h (columns 32h..32h+31)
+                    // that belong to a diagonal block lie in rows 32h..32h+31, which are the
+                    // TMEM lanes of the warps with (sp & 1) == h.  The other warps skip the
+                    // region but still wait for it and report it drained, so every mbarrier
+                    // phase keeps its arrival count; the write-out reads diagonal entries only.
+                    const bool useful = !PACK || lmt == 6 || (sp & 1) == h;
                     uint64_t acc[16];
 #pragma unroll
                     for (int u = 0; u < 16; u++) acc[u] = 0;
-                    if (mbar_wait(&tfull[h], p & 1, abort)) {
+                    if (mbar_wait(&tfull[h], p & 1, abort) && useful) {
                         asm volatile("tcgen05.fence::after_thread_sync;");
 #pragma unroll
                         for (int s = 0; s < 2; s++) {
@@ -631,13 +637,15 @@ pw_f16_kernel(PwArgs a)
                     }
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&tempty[h]);
-                    uint32_t r[16];
+                    if (useful) {
+                        uint32_t r[16];
 #pragma unroll
-                    for (int u = 0; u < 16; u++) r[u] = mod64_q_2(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
+                        for (int u = 0; u < 16; u++) r[u] = mod64_q_2(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
 #pragma unroll
-                    for (int m = 0; m < 4; m++)
-                        *reinterpret_cast<uint4 *>(row + 32 * h + 16 * ch + 4 * m) =
-                            make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                        for (int m = 0; m < 4; m++)
+                            *reinterpret_cast<uint4 *>(row + 32 * h + 16 * ch + 4 * m) =
+                                make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
+                    }
                 }
             }
             asm volatile("bar.sync 1, %0;" ::"n"(F16_EPI_WARPS * 32) : "memory");
