@@ -437,7 +437,7 @@ __device__ __forceinline__ uint2 f16_load_pair(const PwOperand &op, int64_t e, i
     return v;
 }
 
-template <bool TILE, bool PACK>
+template <bool TILE, bool PACK, bool SKIP>
 __global__ void __launch_bounds__(F16_THREADS, 1)
 pw_f16_kernel(PwArgs a)
 {
@@ -604,17 +604,22 @@ pw_f16_kernel(PwArgs a)
                 w[s][j] = a.wd[2 * s + hi][j];
                 koff -= 0x4B400000ull * w[s][j];
             }
+        // This warp's outputs in region h are rows 32 (sp & 1) + [0, 32) and columns
+        // 32h + 16ch + [0, 16).  Packed blocks (2^lmt <= 32) have their diagonal outputs
+        // of region h in rows 32h..32h+31, so only warps with (sp & 1) == h hold any;
+        // unpacked, the warp holds some only when its rows and columns meet the r x c
+        // result.  With SKIP (every shape below 64 x 64) a warp without any skips the
+        // region but still waits for it and reports it drained, so every mbarrier phase
+        // keeps its arrival count; the write-out reads only outputs that are in the result.
+        const bool packed = lmt < 6;
+        const bool use0 = !SKIP || (packed ? (sp & 1) == 0 : 32 * (sp & 1) < a.r && 16 * ch < a.c);
+        const bool use1 = !SKIP || (packed ? (sp & 1) == 1 : 32 * (sp & 1) < a.r && 32 + 16 * ch < a.c);
         uint32_t p = 0;
         for (int64_t gc = blockIdx.x; gc < nunits; gc += gridDim.x) {
             for (int pp = 0; pp < 2; pp++, p++) {
                 uint32_t *row = Cst + (pp * 2 + hi) * F16_CST_WORDS + i * F16_CST_LD;
                 for (int h = 0; h < 2; h++) {
-                    // Packed blocks (2^lmt <= 32): the outputs of region h (columns 32h..32h+31)
-                    // that belong to a diagonal block lie in rows 32h..32h+31, which are the
-                    // TMEM lanes of the warps with (sp & 1) == h.  The other warps skip the
-                    // region but still wait for it and report it drained, so every mbarrier
-                    // phase keeps its arrival count; the write-out reads diagonal entries only.
-                    const bool useful = !PACK || lmt == 6 || (sp & 1) == h;
+                    const bool useful = h ? use1 : use0;
                     uint64_t acc[16];
 #pragma unroll
                     for (int u = 0; u < 16; u++) acc[u] = 0;
@@ -757,10 +762,12 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
     if (!attr_done) {
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_i8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i8));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc2));
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
-        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
         attr_done = true;
     }
     if (a.npts <= 0) return PMLG_OK;
@@ -786,14 +793,19 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
         const int64_t g3 = units < ctx->sm_count ? units : ctx->sm_count;
         prof_begin(ctx, "pointwise_f16_tc", st);
         const bool pack = b.lmt < 6;
-        if (tile && !pack)
-            pw_f16_kernel<true, false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        const bool skip = a.r < 64 || a.c < 64;   // some epilogue warps hold no output of a region
+        if (tile && pack)
+            pw_f16_kernel<true, true, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        else if (tile && skip)
+            pw_f16_kernel<true, false, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
         else if (tile)
-            pw_f16_kernel<true, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
-        else if (!pack)
-            pw_f16_kernel<false, false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+            pw_f16_kernel<true, false, false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        else if (pack)
+            pw_f16_kernel<false, true, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+        else if (skip)
+            pw_f16_kernel<false, false, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
         else
-            pw_f16_kernel<false, true><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
+            pw_f16_kernel<false, false, false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
     } else {
         const int64_t items = (a.npts + 1) / 2;
         const int64_t g2 = items < ctx->sm_count ? items : ctx->sm_count;
