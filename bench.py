@@ -363,13 +363,23 @@ def measure_batched_uneven(ctx, dev, st, forms, rank):
     res, outs = {}, {}
     for name, form in forms:
         ctx.set_form(form)
-        ms, out = _time_calls(lambda: pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx), st, 3, 1)
+        # outputs allocated once: the repeated batch is replayed from a CUDA graph
+        bufs = [torch.empty((A.shape[0], B.shape[1], A.shape[2] + B.shape[2] - 1), dtype=torch.int64, device=dev)
+                for A, B, _ in jobs]
+        # two warm-up calls: the first launches directly, the second captures the graph
+        ms, out = _time_calls(lambda: pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx, out=bufs), st, 3, 2)
         res[name + "_ms"] = ms
         outs[name] = out
+        if name == "f16_tc":
+            ctx.set_batch_graphs(False)
+            res[name + "_direct_ms"], _ = _time_calls(
+                lambda: pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx, out=bufs), st, 3, 1)
+            ctx.set_batch_graphs(True)
     ref = outs.get("cuda_core", next(iter(outs.values())))
     res["forms_agree"] = all(all(bool(torch.equal(a, b)) for a, b in zip(ref, o)) for o in outs.values())
     res["config"] = ("256 instances, m uniform in {4..48}, length 2^U(6,12), half p = 998244353, "
-                     "half seeded 59-bit primes (CRT over NTT primes), uniform coefficients")
+                     "half seeded 59-bit primes (CRT over NTT primes), uniform coefficients; "
+                     "repeated calls replay a CUDA graph (*_direct_ms: every kernel launched directly)")
     res["coefficient_macs"] = macs
     return res
 

@@ -51,7 +51,7 @@ enum pmlg_status_code
 /* Which kernel form computes the pointwise matrix products. */
 enum pmlg_form
 {
-    PMLG_FORM_AUTO = 0,       /* library choice (fastest measured) */
+    PMLG_FORM_AUTO = 0,       /* per shape class, the form measured fastest (pmlg_ctx_set_tuning) */
     PMLG_FORM_CUDA_CORE = 1,  /* uint64 multiply-accumulate with delayed reduction */
     PMLG_FORM_INT8_TC = 2,    /* 8-bit limbs on the INT8 tensor cores (mma.sync, s32 accumulate) */
     PMLG_FORM_F16_TC = 3      /* exact small signed digits in FP16 on tcgen05 (FP32 accumulate, all
@@ -85,6 +85,16 @@ enum pmlg_poly_mat_form
 PMLG_API int pmlg_ctx_create(pmlg_ctx **ctx, int device);
 PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx);
 PMLG_API int pmlg_ctx_set_form(pmlg_ctx *ctx, int form);
+/* PMLG_FORM_AUTO measures the three forms on the first product of each shape class
+ * (r, k, c, number of points rounded up to a power of two) and keeps the fastest for
+ * the class; on = 0 makes AUTO take the FP16 form without measuring. */
+PMLG_API int pmlg_ctx_set_tuning(pmlg_ctx *ctx, int on);
+/* the form AUTO chose for a shape class, PMLG_FORM_AUTO when none was measured yet,
+ * -PMLG_EINVAL for a shape outside 1..64 */
+PMLG_API int pmlg_ctx_tuned_form(const pmlg_ctx *ctx, int r, int k, int c, int64_t npts);
+/* pmlg_poly_mat_mul_batch: on (the default), a batch called again with the same jobs is
+ * captured into a CUDA graph on its second call and replayed on later ones */
+PMLG_API int pmlg_ctx_set_batch_graphs(pmlg_ctx *ctx, int on);
 /* pmbasis leaf order (mbasis below it); 0 restores the tuned default */
 PMLG_API int pmlg_ctx_set_leaf_order(pmlg_ctx *ctx, int64_t order);
 /* number of kernels this context has launched so far */

@@ -57,6 +57,21 @@ class Context:
     def set_leaf_order(self, order: int) -> None:
         check(self.lib.pmlg_ctx_set_leaf_order(self.handle, order), self.handle)
 
+    def set_tuning(self, on: bool) -> None:
+        """PMLG_FORM_AUTO measures the forms per shape class (on) or takes FP16 (off)."""
+        check(self.lib.pmlg_ctx_set_tuning(self.handle, 1 if on else 0), self.handle)
+
+    def tuned_form(self, r: int, k: int, c: int, npts: int) -> int:
+        """The form AUTO chose for the shape class, 0 (PMLG_FORM_AUTO) if not measured yet."""
+        f = self.lib.pmlg_ctx_tuned_form(self.handle, r, k, c, npts)
+        if f < 0:
+            raise ValueError("shape outside 1..64")
+        return f
+
+    def set_batch_graphs(self, on: bool) -> None:
+        """Capture repeated batches into CUDA graphs (on, the default) or launch directly."""
+        check(self.lib.pmlg_ctx_set_batch_graphs(self.handle, 1 if on else 0), self.handle)
+
     @property
     def launches(self) -> int:
         return int(self.lib.pmlg_ctx_launch_count(self.handle))
@@ -202,20 +217,30 @@ def nmod_poly_mat_mulmid(A, B, nlo: int, nhi: int, p: int, ctx: Optional[Context
     return (out, int(n.value)) if want_length else out
 
 
-def nmod_poly_mat_multiply_batch(jobs, ctx: Optional[Context] = None):
+def nmod_poly_mat_multiply_batch(jobs, ctx: Optional[Context] = None, out=None):
     """jobs: list of (A, B, p) with CUDA tensors; returns the list of products,
-    computed by one pmlg_poly_mat_mul_batch call."""
+    computed by one pmlg_poly_mat_mul_batch call.  `out`, a list of contiguous int64
+    CUDA tensors of the products' shapes, receives them instead of new tensors (a batch
+    repeated on the same buffers is replayed from a CUDA graph)."""
     import torch
     if not jobs:
         return []
     ctx = _ctx(ctx, jobs[0][0])
+    if out is not None and len(out) != len(jobs):
+        raise ValueError("out must hold one tensor per job")
     outs = []
     arr = (PolymatJob * len(jobs))()
     for i, (A, B, p) in enumerate(jobs):
         _require_cuda(A, B)
         r, k, l1 = A.shape
         _, c, l2 = B.shape
-        o = torch.empty((r, c, l1 + l2 - 1 if l1 and l2 else 0), dtype=torch.int64, device=A.device)
+        shape = (r, c, l1 + l2 - 1 if l1 and l2 else 0)
+        if out is None:
+            o = torch.empty(shape, dtype=torch.int64, device=A.device)
+        else:
+            o = out[i]
+            if tuple(o.shape) != shape or o.dtype != torch.int64 or not o.is_cuda or not o.is_contiguous():
+                raise ValueError(f"out[{i}] must be a contiguous int64 CUDA tensor of shape {shape}")
         outs.append(o)
         arr[i] = PolymatJob(r, k, c, l1, l2, p, _ptr(A), _ptr(B), _ptr(o))
     ctx.check(ctx.lib.pmlg_poly_mat_mul_batch(ctx.handle, C.cast(arr, C.c_void_p), len(jobs),

@@ -27,6 +27,9 @@ SIGNATURES = {
     "pmlg_ctx_destroy": (C.c_int, [_vp]),
     "pmlg_ctx_set_form": (C.c_int, [_vp, C.c_int]),
     "pmlg_ctx_set_leaf_order": (C.c_int, [_vp, _i64]),
+    "pmlg_ctx_set_tuning": (C.c_int, [_vp, C.c_int]),
+    "pmlg_ctx_tuned_form": (C.c_int, [_vp, C.c_int, C.c_int, C.c_int, _i64]),
+    "pmlg_ctx_set_batch_graphs": (C.c_int, [_vp, C.c_int]),
     "pmlg_ctx_launch_count": (C.c_ulonglong, [_vp]),
     "pmlg_ctx_last_error": (C.c_char_p, [_vp]),
     "pmlg_ctx_device_status": (C.c_int, [_vp, _vp]),

@@ -1,5 +1,6 @@
 // context.cu -- context, scratch memory, NTT tables and CRT plans.
 #include "pmlg_internal.cuh"
+#include "pointwise.cuh"
 
 #include <cstdarg>
 #include <cstdio>
@@ -392,6 +393,8 @@ PMLG_API int pmlg_ctx_destroy(pmlg_ctx *ctx)
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     for (auto &r : ctx->prof) { cudaEventDestroy(r.beg); cudaEventDestroy(r.end); }
     for (auto e : ctx->event_pool) cudaEventDestroy(e);
+    for (auto &g : ctx->bgraph)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     delete ctx;
     return PMLG_OK;
 }
@@ -400,6 +403,28 @@ PMLG_API int pmlg_ctx_set_form(pmlg_ctx *ctx, int form)
 {
     if (!ctx || form < PMLG_FORM_AUTO || form > PMLG_FORM_F16_TC) return PMLG_EINVAL;
     ctx->form = form;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_set_tuning(pmlg_ctx *ctx, int on)
+{
+    if (!ctx) return PMLG_EINVAL;
+    ctx->tuning = on ? 1 : 0;
+    return PMLG_OK;
+}
+
+PMLG_API int pmlg_ctx_tuned_form(const pmlg_ctx *ctx, int r, int k, int c, int64_t npts)
+{
+    if (!ctx || r < 1 || r > 64 || k < 1 || k > 64 || c < 1 || c > 64 || npts < 1) return -PMLG_EINVAL;
+    auto it = ctx->tuned.find(tune_key(r, k, c, npts));
+    return it == ctx->tuned.end() ? PMLG_FORM_AUTO : it->second;
+}
+
+PMLG_API int pmlg_ctx_set_batch_graphs(pmlg_ctx *ctx, int on)
+{
+    if (!ctx) return PMLG_EINVAL;
+    ctx->batch_graphs = on ? 1 : 0;
+    if (!on) ctx->batch_seen = 0;
     return PMLG_OK;
 }
 

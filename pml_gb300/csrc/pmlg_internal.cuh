@@ -14,6 +14,7 @@
 
 #include <cstdint>
 #include <cstddef>
+#include <map>
 #include <vector>
 #include <cuda_runtime.h>
 
@@ -149,6 +150,21 @@ struct pmlg_ctx
     int profiling = 0;
     std::vector<pmlg::ProfRecord> prof;
     std::vector<cudaEvent_t> event_pool;
+    // PMLG_FORM_AUTO: pointwise form chosen per shape class by measurement
+    int tuning = 1;                          // 0: AUTO takes the FP16 form unmeasured
+    std::map<uint64_t, int> tuned;           // shape class -> fastest form measured
+    // batched products: a repeated batch is captured into a CUDA graph and replayed
+    struct BatchGraph
+    {
+        uint64_t key = 0;
+        cudaGraphExec_t exec = nullptr;
+        unsigned long long launches = 0;
+    };
+    static constexpr int kBatchGraphs = 4;
+    int batch_graphs = 1;                    // 0: every batch launches its kernels directly
+    BatchGraph bgraph[kBatchGraphs];
+    int bgraph_next = 0;
+    uint64_t batch_seen = 0;                 // key of the last batch launched directly
 };
 
 namespace pmlg {

@@ -746,20 +746,12 @@ void pointwise_set_modulus(PwArgs &a, uint32_t q, uint32_t scale)
     a.negoff = ((1ull << 56) / q + 1) * q;
 }
 
-// the library's choice: the FP16-digit tensor-core form, measured fastest on every
-// workload here (the headline product, batched 64x64 products, uneven batches, the
-// products inside pmbasis)
-static int form_resolve(int form)
-{
-    return form == PMLG_FORM_AUTO ? PMLG_FORM_F16_TC : form;
-}
-
-int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
+static int pointwise_attrs(pmlg_ctx *ctx)
 {
     static bool attr_done = false;
-    const size_t smem_i8 = (size_t)PW_PPC * 8 * 64 * I8_LD;
-    const size_t smem_cc2 = 2ull * CC2_STAGE * sizeof(uint32_t);
     if (!attr_done) {
+        const size_t smem_i8 = (size_t)PW_PPC * 8 * 64 * I8_LD;
+        const size_t smem_cc2 = 2ull * CC2_STAGE * sizeof(uint32_t);
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_i8_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_i8));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_cc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_cc2));
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
@@ -770,11 +762,16 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
         PMLG_CUDA_TRY(cudaFuncSetAttribute(pw_f16_kernel<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, F16_SMEM));
         attr_done = true;
     }
-    if (a.npts <= 0) return PMLG_OK;
+    return PMLG_OK;
+}
+
+// one launch of the pointwise products in the given (concrete) form
+static int pointwise_run(pmlg_ctx *ctx, const PwArgs &a, int f, cudaStream_t st)
+{
     const int64_t grid = (a.npts + PW_PPC - 1) / PW_PPC;
     if (grid > 0x7fffffffll) return PMLG_EUNSUP;
-    const int f = form_resolve(form);
     if (f == PMLG_FORM_INT8_TC) {
+        const size_t smem_i8 = (size_t)PW_PPC * 8 * 64 * I8_LD;
         prof_begin(ctx, "pointwise_int8_tc", st);
         pw_i8_kernel<<<(unsigned)grid, PW_THREADS, smem_i8, st>>>(a);
     } else if (f == PMLG_FORM_F16_TC) {
@@ -807,6 +804,7 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
         else
             pw_f16_kernel<false, false, false><<<(unsigned)g3, F16_THREADS, F16_SMEM, st>>>(b);
     } else {
+        const size_t smem_cc2 = 2ull * CC2_STAGE * sizeof(uint32_t);
         const int64_t items = (a.npts + 1) / 2;
         const int64_t g2 = items < ctx->sm_count ? items : ctx->sm_count;
         prof_begin(ctx, "pointwise_cuda_core", st);
@@ -816,6 +814,68 @@ int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
     return PMLG_OK;
+}
+
+uint64_t tune_key(int r, int k, int c, int64_t npts)
+{
+    int lp = 0;
+    while (lp < 62 && (1ll << lp) < npts) lp++;
+    return ((uint64_t)r << 32) | ((uint64_t)k << 24) | ((uint64_t)c << 16) | (uint64_t)lp;
+}
+
+// PMLG_FORM_AUTO: the form measured fastest for this shape class (r, k, c and the
+// number of points rounded up to a power of two).  The first product of a class runs
+// each of the three forms twice on its own data, timed by events on its stream, and
+// keeps the fastest; every form writes the same bits, so the output is right whichever
+// ran last.  No measurement while the stream is being captured, when the products
+// accumulate into C, under per-kernel profiling, or with tuning switched off: the FP16
+// form, fastest on every large workload, is taken then.
+static int pointwise_auto(pmlg_ctx *ctx, const PwArgs &a, cudaStream_t st)
+{
+    const uint64_t key = tune_key(a.r, a.k, a.c, a.npts);
+    auto it = ctx->tuned.find(key);
+    if (it != ctx->tuned.end()) return pointwise_run(ctx, a, it->second, st);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PMLG_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (!ctx->tuning || a.accumulate || ctx->profiling || cs != cudaStreamCaptureStatusNone)
+        return pointwise_run(ctx, a, PMLG_FORM_F16_TC, st);
+    static const int forms[3] = {PMLG_FORM_CUDA_CORE, PMLG_FORM_INT8_TC, PMLG_FORM_F16_TC};
+    cudaEvent_t ev[7] = {};
+    int s = PMLG_OK;
+    for (int i = 0; i < 7 && s == PMLG_OK; i++)
+        if (cudaEventCreate(&ev[i]) != cudaSuccess) s = PMLG_ECUDA;
+    if (s == PMLG_OK && cudaEventRecord(ev[0], st) != cudaSuccess) s = PMLG_ECUDA;
+    for (int f = 0; f < 3 && s == PMLG_OK; f++) {
+        // a first run of each form, then the timed one
+        s = pointwise_run(ctx, a, forms[f], st);
+        if (s == PMLG_OK && cudaEventRecord(ev[1 + 2 * f], st) != cudaSuccess) s = PMLG_ECUDA;
+        if (s == PMLG_OK) s = pointwise_run(ctx, a, forms[f], st);
+        if (s == PMLG_OK && cudaEventRecord(ev[2 + 2 * f], st) != cudaSuccess) s = PMLG_ECUDA;
+    }
+    int best = PMLG_FORM_F16_TC;
+    if (s == PMLG_OK && cudaEventSynchronize(ev[6]) == cudaSuccess) {
+        float bt = 0.f;
+        for (int f = 0; f < 3; f++) {
+            float t = 0.f;
+            if (cudaEventElapsedTime(&t, ev[1 + 2 * f], ev[2 + 2 * f]) != cudaSuccess) continue;
+            if (f == 0 || t < bt) { bt = t; best = forms[f]; }
+        }
+        ctx->tuned[key] = best;
+    } else if (s == PMLG_OK) {
+        s = PMLG_ECUDA;
+    }
+    for (int i = 0; i < 7; i++)
+        if (ev[i]) cudaEventDestroy(ev[i]);
+    if (s == PMLG_ECUDA) set_error(ctx, "pointwise form tuning: an event operation failed");
+    return s;
+}
+
+int pointwise_launch(pmlg_ctx *ctx, const PwArgs &a, int form, cudaStream_t st)
+{
+    PMLG_TRY(pointwise_attrs(ctx));
+    if (a.npts <= 0) return PMLG_OK;
+    if (form == PMLG_FORM_AUTO) return pointwise_auto(ctx, a, st);
+    return pointwise_run(ctx, a, form, st);
 }
 
 int pointwise_blocked(pmlg_ctx *ctx, PwArgs a, int64_t r, int64_t k, int64_t c, int form,

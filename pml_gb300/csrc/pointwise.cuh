@@ -48,4 +48,7 @@ void pointwise_set_modulus(PwArgs &a, uint32_t q, uint32_t scale = 1);
 int pointwise_blocked(pmlg_ctx *ctx, PwArgs a, int64_t r, int64_t k, int64_t c, int form,
                       cudaStream_t st);
 
+// Shape class of the form tuner: r, k, c (each <= 64) and npts rounded up to a power of two.
+uint64_t tune_key(int r, int k, int c, int64_t npts);
+
 }  // namespace pmlg

@@ -584,17 +584,81 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
     PMLG_TRY(ws_reserve(ctx, &ctx->ws_batch, total));
     PMLG_TRY(ensure_side_streams(ctx, K));
     // 3. fork from the caller's stream, run, join back
-    PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[K], st));
-    for (int s = 0; s < K; s++) PMLG_CUDA_TRY(cudaStreamWaitEvent(ctx->bstream[s], ctx->bevent[K], 0));
     char *base = (char *)ctx->ws_batch.ptr;
-    for (int idx : order) {
-        const int s = slot[idx];
-        PMLG_TRY(product_run(ctx, items[idx].j, items[idx].plan, base + off[s], ctx->form, ctx->bstream[s]));
+    auto launch_all = [&]() -> int {
+        PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[K], st));
+        for (int s = 0; s < K; s++) PMLG_CUDA_TRY(cudaStreamWaitEvent(ctx->bstream[s], ctx->bevent[K], 0));
+        for (int idx : order) {
+            const int s = slot[idx];
+            PMLG_TRY(product_run(ctx, items[idx].j, items[idx].plan, base + off[s], ctx->form, ctx->bstream[s]));
+        }
+        for (int s = 0; s < K; s++) {
+            PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[s], ctx->bstream[s]));
+            PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ctx->bevent[s], 0));
+        }
+        return PMLG_OK;
+    };
+    // A batch seen again (same jobs, pointers, moduli, form and scratch) is captured
+    // into a CUDA graph on its second call and replayed from then on: one launch of the
+    // whole fork / products / join instead of one per kernel.  The first call of a batch
+    // launches directly (it also builds every table and tunes every form the batch needs,
+    // host work that a capture must not contain).
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    PMLG_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (!ctx->batch_graphs || ctx->profiling || cs != cudaStreamCaptureStatusNone) return launch_all();
+    uint64_t key = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int b = 0; b < 8; b++) {
+            key ^= (v >> (8 * b)) & 0xff;
+            key *= 1099511628211ull;
+        }
+    };
+    mix((uint64_t)njobs); mix((uint64_t)ctx->form); mix((uint64_t)(uintptr_t)base); mix((uint64_t)total);
+    mix((uint64_t)(uintptr_t)st);
+    for (int64_t i = 0; i < njobs; i++) {
+        const pmlg_polymat_job &J = jobs[i];
+        mix((uint64_t)(uintptr_t)J.C); mix((uint64_t)(uintptr_t)J.A); mix((uint64_t)(uintptr_t)J.B);
+        mix((uint64_t)J.r); mix((uint64_t)J.k); mix((uint64_t)J.c); mix((uint64_t)J.len1); mix((uint64_t)J.len2);
+        mix(J.p);
     }
-    for (int s = 0; s < K; s++) {
-        PMLG_CUDA_TRY(cudaEventRecord(ctx->bevent[s], ctx->bstream[s]));
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, ctx->bevent[s], 0));
+    for (auto &g : ctx->bgraph)
+        if (g.exec && g.key == key) {
+            PMLG_CUDA_TRY(cudaGraphLaunch(g.exec, st));
+            count_launch(ctx, (unsigned)g.launches);
+            return PMLG_OK;
+        }
+    if (ctx->batch_seen != key) {
+        ctx->batch_seen = key;
+        return launch_all();
     }
+    // second call of this batch: capture, instantiate, launch
+    const unsigned long long l0 = ctx->launches;
+    cudaGraph_t graph = nullptr;
+    int s = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess ? PMLG_OK : PMLG_ECUDA;
+    if (s == PMLG_OK) {
+        s = launch_all();
+        if (cudaStreamEndCapture(st, &graph) != cudaSuccess && s == PMLG_OK) s = PMLG_ECUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    if (s == PMLG_OK && graph && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) s = PMLG_ECUDA;
+    if (graph) cudaGraphDestroy(graph);
+    const unsigned long long recorded = ctx->launches - l0;   // kernels the capture recorded
+    ctx->launches = l0;
+    if (s != PMLG_OK || !exec) {
+        // the capture failed: clear its error and launch directly
+        (void)cudaGetLastError();
+        if (exec) cudaGraphExecDestroy(exec);
+        ctx->batch_graphs = 0;
+        return launch_all();
+    }
+    pmlg_ctx::BatchGraph &slotg = ctx->bgraph[ctx->bgraph_next];
+    ctx->bgraph_next = (ctx->bgraph_next + 1) % pmlg_ctx::kBatchGraphs;
+    if (slotg.exec) cudaGraphExecDestroy(slotg.exec);
+    slotg.exec = exec;
+    slotg.key = key;
+    slotg.launches = recorded;
+    PMLG_CUDA_TRY(cudaGraphLaunch(exec, st));
+    count_launch(ctx, (unsigned)slotg.launches);
     return PMLG_OK;
 }
 

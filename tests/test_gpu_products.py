@@ -118,11 +118,9 @@ def test_products_random(fctx, dims, p):
                                   (1, 1, 1, 2048, 2048)])
 @pytest.mark.parametrize("p", [P998, 2305843009213693951, 18446744073709551557])
 def test_products_large_transforms(fctx, dims, p):
-    """Transform lengths 4096 to 16384, where the forward transforms of operands of at
-    most N/2 coefficients run persistently with their next coefficients staged in
-    shared memory (as 32-bit words for p = 998244353, whole 64-bit words when the
-    coefficients need reduction modulo each CRT prime), and longer operands take the
-    one-transform-per-CTA kernel: bit-exact against the oracle."""
+    """Transform lengths 4096 to 16384 (the TMA-store forward and the persistent inverse
+    transforms), with operands of at most and of more than half the transform, moduli
+    that take one NTT prime or CRT over several: bit-exact against the oracle."""
     r, k, c, l1, l2 = dims
     A = oracle.rand_poly_mat(r, k, l1, p, 31)
     B = oracle.rand_poly_mat(k, c, l2, p, 32)
@@ -268,3 +266,74 @@ def test_host_path_row_blocks(ctx, dims, prime):
     assert np.array_equal(Ch, oracle.poly_mat_mul(A, B, p, nthreads=8))
     Cd = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), p, ctx=ctx))
     assert np.array_equal(Ch, Cd)
+
+
+def test_form_tuner(ctx):
+    """PMLG_FORM_AUTO measures the three forms on the first product of a shape class and
+    keeps the fastest: the result is exact on the measuring call and after it, and the
+    chosen form is one of the three."""
+    import pml_gb300
+    p = P998
+    ctx.set_form(0)
+    A = oracle.rand_poly_mat(24, 20, 60, p, 71)
+    B = oracle.rand_poly_mat(20, 28, 65, p, 72)
+    ref = oracle.poly_mat_mul(A, B, p, nthreads=8)
+    assert ctx.tuned_form(24, 20, 28, 128) == 0
+    for _ in range(2):
+        assert np.array_equal(to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A), to_dev(B), p, ctx=ctx)), ref)
+    assert ctx.tuned_form(24, 20, 28, 128) in (1, 2, 3)
+    # switched off: AUTO takes the FP16 form for a new class, still exact
+    ctx.set_tuning(False)
+    A2 = oracle.rand_poly_mat(9, 9, 40, p, 73)
+    B2 = oracle.rand_poly_mat(9, 9, 40, p, 74)
+    out = to_host(pml_gb300.nmod_poly_mat_multiply(to_dev(A2), to_dev(B2), p, ctx=ctx))
+    assert np.array_equal(out, oracle.poly_mat_mul(A2, B2, p, nthreads=8))
+    assert ctx.tuned_form(9, 9, 9, 128) == 0
+    ctx.set_tuning(True)
+    with pytest.raises(ValueError):
+        ctx.tuned_form(65, 1, 1, 8)
+
+
+@pytest.mark.parametrize("form", [0, 3, 1])
+def test_batch_graph_replay(ctx, form):
+    """A batch called again is captured into a CUDA graph and replayed: every call is
+    exact, the replay reads the inputs' current contents, each call counts the same
+    number of kernels, and a changed job or graphs switched off launch directly."""
+    import pml_gb300
+    import torch
+    rng = np.random.default_rng(80 + form)
+    ctx.set_form(form)
+    shapes = [(3, 5, 4, 30, 40, P998), (8, 8, 8, 100, 90, 2305843009213693951), (1, 7, 2, 5, 300, 1000003),
+              (16, 16, 16, 64, 64, P998)]
+    As, Bs, refs, jobs = [], [], [], []
+    for i, (r, k, c, l1, l2, p) in enumerate(shapes):
+        A = oracle.rand_poly_mat(r, k, l1, p, 90 + i)
+        B = oracle.rand_poly_mat(k, c, l2, p, 95 + i)
+        As.append(to_dev(A)); Bs.append(to_dev(B))
+        refs.append(oracle.poly_mat_mul(A, B, p, nthreads=8))
+        jobs.append((As[-1], Bs[-1], p))
+    outs = [torch.zeros((r, c, l1 + l2 - 1), dtype=torch.int64, device="cuda") for (r, k, c, l1, l2, p) in shapes]
+    counts = []
+    for call in range(4):
+        l0 = ctx.launches
+        pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx, out=outs)
+        torch.cuda.synchronize()
+        counts.append(ctx.launches - l0)
+        assert all(np.array_equal(to_host(o), r) for o, r in zip(outs, refs)), call
+    assert len(set(counts[1:])) == 1
+    # new contents in the same buffers: the replayed graph reads them
+    r, k, c, l1, l2, p = shapes[0]
+    A = oracle.rand_poly_mat(r, k, l1, p, 123)
+    As[0].copy_(to_dev(A))
+    refs[0] = oracle.poly_mat_mul(A, to_host(Bs[0]), p, nthreads=8)
+    pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx, out=outs)
+    assert all(np.array_equal(to_host(o), rr) for o, rr in zip(outs, refs))
+    # graphs off: direct launches, same results
+    ctx.set_batch_graphs(False)
+    for o in outs:
+        o.zero_()
+    pml_gb300.nmod_poly_mat_multiply_batch(jobs, ctx=ctx, out=outs)
+    assert all(np.array_equal(to_host(o), rr) for o, rr in zip(outs, refs))
+    ctx.set_batch_graphs(True)
+    ctx.set_form(0)
+
