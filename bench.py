@@ -56,11 +56,12 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the pointwise-batch and batched-uneven measurements")
-    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven", "kernel", "layout"],
+    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven", "kernel", "layout", "dot"],
                     default=None,
                     help="run one product per form (or one pmbasis at order 1024, one 4096-product "
                          "pointwise batch per form, one batched-uneven call with the FP16 form, one kernel "
-                         "basis of a 64x32 degree-255 matrix, one layout conversion each way at 64x64 x 4096) "
+                         "basis of a 64x32 degree-255 matrix, one layout conversion each way at 64x64 x 4096, "
+                         "one call of each dot-product kernel on about 256 MB) "
                          "and exit: the small cases for kernel captures")
     return ap.parse_args()
 
@@ -99,6 +100,12 @@ def run_profile_case(args):
         ker, piv, rdeg = pml_gb300.nmod_poly_mat_kernel(F, [0] * 64, P, ctx=ctx)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "kernel", "nullity": int(ker.shape[0]), "launches": ctx.launches}))
+    elif args.profile_case == "dot":
+        import torch
+        for name, (a, b, p, nbytes) in _dot_inputs(torch.device("cuda", 0), 61, shift=2).items():
+            _dot_call(ctx, name, a, b, p)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "dot", "launches": ctx.launches}))
     elif args.profile_case == "layout":
         rng = np.random.default_rng(31)
         Pm = torch.from_numpy(rng.integers(0, P, size=(64, 64, 4096), dtype=np.uint64).view(np.int64)).cuda()
@@ -407,6 +414,63 @@ def measure_kernel_basis(ctx, dev, st, rank):
             "timing": "wall clock around one call after one warm-up call"}
 
 
+def _dot_inputs(dev, seed: int, shift: int = 0):
+    """About 1 GB >> shift of operands per dot-product kernel (larger than L2 for shift <= 2,
+    no flush needed)."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    # entries in [0, hi) drawn as int64; 32-bit operands keep the low 32 bits of each
+    rnd = lambda n, dt, hi: torch.randint(0, hi, (n,), dtype=torch.int64, device=dev, generator=g).to(dt)
+    p64, p32 = 2 ** 61 - 1, 4294967291
+    n64, n32, rows = 1 << (26 - shift), 1 << (27 - shift), 8192 >> shift
+    return {
+        "dot64": (rnd(n64, torch.int64, p64), rnd(n64, torch.int64, p64), p64, 16 * n64),
+        "dot32": (rnd(n32, torch.int32, p32), rnd(n32, torch.int32, p32), p32, 8 * n32),
+        "mdot32": (rnd(rows * 32768, torch.int32, p32).view(rows, 32768), rnd(32768, torch.int32, p32), p32,
+                   4 * rows * 32768 + 4 * 32768),
+        "dot_multi": (rnd(rows // 2, torch.int64, p64), rnd(rows // 2 * 32768, torch.int64, p64).view(rows // 2, 32768),
+                      p64, 8 * (rows // 2) * 32768 + 8 * (rows // 2)),
+    }
+
+
+def _dot_call(ctx, name, a, b, p):
+    import pml_gb300
+    if name == "dot64":
+        return pml_gb300.nmod_vec_dot_product(a, b, p, ctx=ctx)
+    if name == "dot32":
+        return pml_gb300.nmod32_vec_dot_product(a, b, p, ctx=ctx)
+    if name == "mdot32":
+        return pml_gb300.nmod32_vec_mdot(a, b, p, ctx=ctx)
+    return pml_gb300.nmod_vec_dot_product_multi(a, b, p, ctx=ctx)
+
+
+def measure_dot_products(ctx, dev, st, rank, peak_gbs):
+    """The modular dot products (nmod_vec_dot_product_unbalanced, _nmod32_vec_dot_split,
+    _nmod32_vec_mdot_split, nmod_vec_dot_product_multi) on about 1 GB of operands each:
+    device time of the kernels (CUDA events through the context's profiling), algorithmic
+    bytes = every operand entry read once, as a fraction of the measured HBM copy rate."""
+    import torch
+    res = {}
+    for name, (a, b, p, nbytes) in _dot_inputs(dev, 61 + rank).items():
+        for _ in range(3):
+            _dot_call(ctx, name, a, b, p)
+        torch.cuda.synchronize()
+        ctx.set_profiling(True)
+        for _ in range(10):
+            _dot_call(ctx, name, a, b, p)
+        torch.cuda.synchronize()
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        us = sum(v[0] for v in prof.values()) / 10 * 1e3
+        gbs = nbytes / us / 1e3
+        res[name] = {"us": us, "gbs": gbs, "frac_of_measured_hbm": gbs / peak_gbs if peak_gbs else None,
+                     "bytes": nbytes, "kernels": sorted(prof)}
+    res["config"] = ("dot64: 2^26 entries mod 2^61-1; dot32: 2^27 entries mod 4294967291; mdot32: 8192 x 32768 "
+                     "matrix times vector; dot_multi: 4096-vector times 4096 x 32768 matrix")
+    return res
+
+
 def measure_layout(ctx, dev, st, rank, peak_gbs):
     """Entry-major -> coefficient-major and back for a 64x64 matrix of length 4096
     (nmod_mat_poly_set_trunc_from_poly_mat / nmod_poly_mat_set_trunc_from_mat_poly):
@@ -673,6 +737,7 @@ def run_pml(args):
         "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
         "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
         "layout_conversion": measure_layout(ctx, dev, st, rank, peaks.get("hbm_gbs")),
+        "dot_products": measure_dot_products(ctx, dev, st, rank, peaks.get("hbm_gbs")),
         "dixon": measure_dixon(ctx, dev, st, rank),
         "popov_pmbasis": measure_popov(ctx, dev, st, rank),
     }

@@ -78,14 +78,71 @@ __device__ __forceinline__ uint64_t mod192(const U192 &v, uint64_t p)
     return (uint64_t)acc;
 }
 
+// Streaming loads: every element is read once, so L1 keeps none of it.
+__device__ __forceinline__ ulonglong2 ld_nc2(const ulonglong2 *p)
+{
+    ulonglong2 v;
+    asm("ld.global.nc.L1::no_allocate.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint4 ld_nc4(const uint4 *p)
+{
+    uint4 v;
+    asm("ld.global.nc.L1::no_allocate.v4.u32 {%0, %1, %2, %3}, [%4];"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void mac64(U192 &acc, unsigned long long a, unsigned long long b)
+{
+    add128(acc, a * b, __umul64hi(a, b));
+}
+
+// HBM-bound: with 16-byte vectors of both operands and four of each in flight per
+// thread (grid-strided), the loads outstanding cover the latency of the memory system.
+constexpr int DOT_UNROLL = 4;
+
+#ifndef PMLG_DOTMULTI_PAIRS
+#define PMLG_DOTMULTI_PAIRS 1          // vector-matrix products: two columns per thread
+#endif
+#ifndef PMLG_DOTMULTI_BLOCKS_PER_SM
+#define PMLG_DOTMULTI_BLOCKS_PER_SM 32  // target blocks per SM (row chunks x column blocks)
+#endif
+
 __global__ void dot64_partial(const uint64_t *__restrict__ v1, const uint64_t *__restrict__ v2, int64_t len,
                               U192 *part)
 {
     U192 acc{0, 0, 0};
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t a = v1[i], b = v2[i];
-        add128(acc, a * b, __umul64hi(a, b));
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t start = 0;
+    if (((reinterpret_cast<uintptr_t>(v1) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0) {
+        const ulonglong2 *a2 = reinterpret_cast<const ulonglong2 *>(v1);
+        const ulonglong2 *b2 = reinterpret_cast<const ulonglong2 *>(v2);
+        const int64_t n2 = len >> 1;
+        int64_t i = tid;
+        for (; i + (DOT_UNROLL - 1) * stride < n2; i += DOT_UNROLL * stride) {
+            ulonglong2 a[DOT_UNROLL], b[DOT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < DOT_UNROLL; u++) {
+                a[u] = ld_nc2(a2 + i + u * stride);
+                b[u] = ld_nc2(b2 + i + u * stride);
+            }
+#pragma unroll
+            for (int u = 0; u < DOT_UNROLL; u++) {
+                mac64(acc, a[u].x, b[u].x);
+                mac64(acc, a[u].y, b[u].y);
+            }
+        }
+        for (; i < n2; i += stride) {
+            const ulonglong2 a = ld_nc2(a2 + i), b = ld_nc2(b2 + i);
+            mac64(acc, a.x, b.x);
+            mac64(acc, a.y, b.y);
+        }
+        start = n2 << 1;
     }
+    for (int64_t i = start + tid; i < len; i += stride) mac64(acc, v1[i], v2[i]);
     acc = block_sum192(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
@@ -95,15 +152,31 @@ __global__ void dot32_partial(const uint32_t *__restrict__ v1, const uint32_t *_
 {
     // products < 2^64: accumulate in 64 bits and carry into the high words
     U192 acc{0, 0, 0};
-    const int64_t n4 = len >> 2;
-    const uint4 *a4 = reinterpret_cast<const uint4 *>(v1);
-    const uint4 *b4 = reinterpret_cast<const uint4 *>(v2);
-    const bool vec = ((reinterpret_cast<uintptr_t>(v1) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t start = 0;
-    if (vec) {
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-            const uint4 a = a4[i], b = b4[i];
+    if (((reinterpret_cast<uintptr_t>(v1) | reinterpret_cast<uintptr_t>(v2)) & 15) == 0) {
+        const uint4 *a4 = reinterpret_cast<const uint4 *>(v1);
+        const uint4 *b4 = reinterpret_cast<const uint4 *>(v2);
+        const int64_t n4 = len >> 2;
+        int64_t i = tid;
+        for (; i + (DOT_UNROLL - 1) * stride < n4; i += DOT_UNROLL * stride) {
+            uint4 a[DOT_UNROLL], b[DOT_UNROLL];
+#pragma unroll
+            for (int u = 0; u < DOT_UNROLL; u++) {
+                a[u] = ld_nc4(a4 + i + u * stride);
+                b[u] = ld_nc4(b4 + i + u * stride);
+            }
+#pragma unroll
+            for (int u = 0; u < DOT_UNROLL; u++) {
+                add128(acc, (uint64_t)a[u].x * b[u].x, 0);
+                add128(acc, (uint64_t)a[u].y * b[u].y, 0);
+                add128(acc, (uint64_t)a[u].z * b[u].z, 0);
+                add128(acc, (uint64_t)a[u].w * b[u].w, 0);
+            }
+        }
+        for (; i < n4; i += stride) {
+            const uint4 a = ld_nc4(a4 + i), b = ld_nc4(b4 + i);
             add128(acc, (uint64_t)a.x * b.x, 0);
             add128(acc, (uint64_t)a.y * b.y, 0);
             add128(acc, (uint64_t)a.z * b.z, 0);
@@ -111,8 +184,7 @@ __global__ void dot32_partial(const uint32_t *__restrict__ v1, const uint32_t *_
         }
         start = n4 << 2;
     }
-    for (int64_t i = start + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < len; i += stride)
-        add128(acc, (uint64_t)v1[i] * v2[i], 0);
+    for (int64_t i = start + tid; i < len; i += stride) add128(acc, (uint64_t)v1[i] * v2[i], 0);
     acc = block_sum192(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = acc;
 }
@@ -146,7 +218,23 @@ __global__ void mdot32_kernel(uint32_t *mv, const uint32_t *__restrict__ mat, co
     if (lane == 0) mv[warp] = (uint32_t)mod192(acc, p);
 }
 
-// uv[j] = sum_i u[i] * v[i*k + j]: grid.x over columns, grid.y over chunks of i
+// one 256-thread block per row, for rows of at least 4096 entries: sixteen times
+// more (and shorter) tasks than rows of one warp, so the last wave of a tall matrix
+// leaves few SMs idle
+constexpr int MDOT_BLOCK = 256;
+__global__ void __launch_bounds__(MDOT_BLOCK)
+mdot32_block_kernel(uint32_t *mv, const uint32_t *__restrict__ mat, const uint32_t *__restrict__ vec,
+                    int64_t len, int64_t stride, uint64_t p)
+{
+    const uint32_t *row = mat + (int64_t)blockIdx.x * stride;
+    U192 acc{0, 0, 0};
+    for (int64_t j = threadIdx.x; j < len; j += MDOT_BLOCK) add128(acc, (uint64_t)row[j] * vec[j], 0);
+    acc = block_sum192(acc);
+    if (threadIdx.x == 0) mv[blockIdx.x] = (uint32_t)mod192(acc, p);
+}
+
+// uv[j] = sum_i u[i] * v[i*k + j]: grid.x over columns, grid.y over chunks of i; eight
+// rows of v in flight per thread
 __global__ void dot_multi_partial(const uint64_t *__restrict__ u, const uint64_t *__restrict__ v, int64_t len,
                                   int64_t k, int64_t chunk, U192 *part)
 {
@@ -155,11 +243,55 @@ __global__ void dot_multi_partial(const uint64_t *__restrict__ u, const uint64_t
     const int64_t i0 = (int64_t)blockIdx.y * chunk;
     const int64_t i1 = i0 + chunk < len ? i0 + chunk : len;
     U192 acc{0, 0, 0};
-    for (int64_t i = i0; i < i1; i++) {
-        const uint64_t a = u[i], b = v[i * k + j];
-        add128(acc, a * b, __umul64hi(a, b));
+    int64_t i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        uint64_t a[8], b[8];
+#pragma unroll
+        for (int t = 0; t < 8; t++) {
+            a[t] = __ldg(u + i + t);
+            b[t] = v[(i + t) * k + j];
+        }
+#pragma unroll
+        for (int t = 0; t < 8; t++) mac64(acc, a[t], b[t]);
     }
+    for (; i < i1; i++) mac64(acc, u[i], v[i * k + j]);
     part[(int64_t)blockIdx.y * k + j] = acc;
+}
+
+// the same, two adjacent columns per thread (k even, v 16-byte aligned): 16-byte loads,
+// four rows in flight
+__global__ void dot_multi_partial2(const uint64_t *__restrict__ u, const uint64_t *__restrict__ v, int64_t len,
+                                   int64_t k, int64_t chunk, U192 *part)
+{
+    const int64_t j2 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;   // column pair
+    if (2 * j2 >= k) return;
+    const int64_t i0 = (int64_t)blockIdx.y * chunk;
+    const int64_t i1 = i0 + chunk < len ? i0 + chunk : len;
+    const ulonglong2 *v2 = reinterpret_cast<const ulonglong2 *>(v);
+    const int64_t k2 = k >> 1;
+    U192 acc0{0, 0, 0}, acc1{0, 0, 0};
+    int64_t i = i0;
+    for (; i + 4 <= i1; i += 4) {
+        uint64_t a[4];
+        ulonglong2 b[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            a[t] = __ldg(u + i + t);
+            b[t] = ld_nc2(v2 + (i + t) * k2 + j2);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+            mac64(acc0, a[t], b[t].x);
+            mac64(acc1, a[t], b[t].y);
+        }
+    }
+    for (; i < i1; i++) {
+        const ulonglong2 b = ld_nc2(v2 + i * k2 + j2);
+        mac64(acc0, u[i], b.x);
+        mac64(acc1, u[i], b.y);
+    }
+    part[(int64_t)blockIdx.y * k + 2 * j2] = acc0;
+    part[(int64_t)blockIdx.y * k + 2 * j2 + 1] = acc1;
 }
 
 __global__ void dot_multi_final(const U192 *part, int64_t nchunks, int64_t k, uint64_t p, uint64_t *uv)
@@ -293,10 +425,14 @@ PMLG_API int pmlg_nmod32_vec_mdot(pmlg_ctx *ctx, uint32_t *mv, const uint32_t *m
     if (p < 2 || p > (1ull << 32)) return PMLG_EBADMOD;
     cudaStream_t st = (cudaStream_t)stream;
     PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
-    const int threads = 256;
-    const int64_t blocks = (nrows * 32 + threads - 1) / threads;
     prof_begin(ctx, "mdot32", st);
-    mdot32_kernel<<<(unsigned)blocks, threads, 0, st>>>(mv, mat, vec, nrows, len, stride, p);
+    if (len >= 4096 && nrows <= 0x7fffffffll) {
+        mdot32_block_kernel<<<(unsigned)nrows, MDOT_BLOCK, 0, st>>>(mv, mat, vec, len, stride, p);
+    } else {
+        const int threads = 256;
+        const int64_t blocks = (nrows * 32 + threads - 1) / threads;
+        mdot32_kernel<<<(unsigned)blocks, threads, 0, st>>>(mv, mat, vec, nrows, len, stride, p);
+    }
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
@@ -313,9 +449,10 @@ PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t
     cudaStream_t st = (cudaStream_t)stream;
     PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
     const int threads = 128;
-    const int64_t gx = (k + threads - 1) / threads;
+    const bool pairs = PMLG_DOTMULTI_PAIRS && (k & 1) == 0 && (reinterpret_cast<uintptr_t>(v) & 15) == 0;
+    const int64_t gx = ((pairs ? k / 2 : k) + threads - 1) / threads;
     // enough chunks along i to fill the GPU, each at least 64 rows long
-    int64_t nchunks = ((int64_t)ctx->sm_count * 8 + gx - 1) / gx;
+    int64_t nchunks = ((int64_t)ctx->sm_count * PMLG_DOTMULTI_BLOCKS_PER_SM + gx - 1) / gx;
     if (nchunks > (len + 63) / 64) nchunks = (len + 63) / 64;
     if (nchunks < 1) nchunks = 1;
     if (nchunks > 65535) nchunks = 65535;
@@ -323,10 +460,13 @@ PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t
     PMLG_TRY(ws_reserve(ctx, &ctx->ws_aux, sizeof(U192) * (size_t)(nchunks * k) + 256));
     U192 *part = (U192 *)ctx->ws_aux.ptr;
     prof_begin(ctx, "dot_multi_partial", st);
-    dot_multi_partial<<<dim3((unsigned)gx, (unsigned)nchunks), threads, 0, st>>>(u, v, len, k, chunk, part);
+    if (pairs)
+        dot_multi_partial2<<<dim3((unsigned)gx, (unsigned)nchunks), threads, 0, st>>>(u, v, len, k, chunk, part);
+    else
+        dot_multi_partial<<<dim3((unsigned)gx, (unsigned)nchunks), threads, 0, st>>>(u, v, len, k, chunk, part);
     prof_end(ctx, st);
     prof_begin(ctx, "dot_multi_final", st);
-    dot_multi_final<<<(unsigned)gx, threads, 0, st>>>(part, nchunks, k, p, uv);
+    dot_multi_final<<<(unsigned)((k + threads - 1) / threads), threads, 0, st>>>(part, nchunks, k, p, uv);
     prof_end(ctx, st);
     count_launch(ctx, 2);
     PMLG_CUDA_TRY(cudaGetLastError());
