@@ -357,6 +357,61 @@ __global__ void multimod_crt_kernel(uint64_t *out, const uint64_t *__restrict__ 
     }
 }
 
+// The same Garner CRT and Horner evaluation without 128-bit division, for p < 2^63
+// (the primes are below 2^63 already): any 64-bit value is reduced by a Barrett step
+// with mq = floor((2^64-1)/q), which leaves at most two subtractions, and every product
+// by a fixed factor w < q is a 64-bit Shoup product with ws = floor(w 2^64 / q), exact
+// for any 64-bit multiplicand and q < 2^63.  All factors and quotients come from the host.
+struct CrtArgs64Fast
+{
+    int t;
+    uint64_t q[kMaxPrimes], mq[kMaxPrimes];
+    uint64_t qlj[kMaxPrimes][kMaxPrimes], qljs[kMaxPrimes][kMaxPrimes];   // q_l mod q_j, l < j
+    uint64_t ginv[kMaxPrimes], ginvs[kMaxPrimes];
+    uint64_t p, mp;
+    uint64_t qlp[kMaxPrimes], qlps[kMaxPrimes];                           // q_l mod p
+};
+
+__device__ __forceinline__ uint64_t red64(uint64_t v, uint64_t q, uint64_t mq)
+{
+    uint64_t r = v - __umul64hi(v, mq) * q;
+    r = r >= q ? r - q : r;
+    return r >= q ? r - q : r;
+}
+
+__device__ __forceinline__ uint64_t shoup64(uint64_t v, uint64_t w, uint64_t ws, uint64_t q)
+{
+    const uint64_t r = v * w - __umul64hi(v, ws) * q;   // in [0, 2q)
+    return r >= q ? r - q : r;
+}
+
+__global__ void multimod_crt_fast_kernel(uint64_t *out, const uint64_t *__restrict__ res, int64_t nb,
+                                         CrtArgs64Fast a)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t c[kMaxPrimes];
+        c[0] = red64(res[i], a.q[0], a.mq[0]);
+        for (int j = 1; j < a.t; j++) {
+            const uint64_t qj = a.q[j], mj = a.mq[j];
+            // c_0 + c_1 q_0 + ... + c_{j-1} q_0 ... q_{j-2} mod q_j, by Horner from the top
+            uint64_t v = red64(c[j - 1], qj, mj);
+            for (int l = j - 2; l >= 0; l--) {
+                v = shoup64(v, a.qlj[l][j], a.qljs[l][j], qj) + red64(c[l], qj, mj);
+                v = v >= qj ? v - qj : v;
+            }
+            const uint64_t r = red64(res[j * nb + i], qj, mj);
+            const uint64_t d = r >= v ? r - v : r + (qj - v);
+            c[j] = shoup64(d, a.ginv[j], a.ginvs[j], qj);
+        }
+        uint64_t x = red64(c[a.t - 1], a.p, a.mp);
+        for (int l = a.t - 2; l >= 0; l--) {
+            x = shoup64(x, a.qlp[l], a.qlps[l], a.p) + red64(c[l], a.p, a.mp);
+            x = x >= a.p ? x - a.p : x;
+        }
+        out[i] = x;
+    }
+}
+
 static int grid_for(pmlg_ctx *ctx, int64_t n, int threads, int per_sm)
 {
     int64_t b = (n + threads - 1) / threads;
@@ -591,7 +646,29 @@ PMLG_API int pmlg_multimod_crt(pmlg_ctx *ctx, uint64_t *out, const uint64_t *res
     cudaStream_t st = (cudaStream_t)stream;
     PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
     prof_begin(ctx, "multimod_crt", st);
-    multimod_crt_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, a);
+    if (p < (1ull << 63)) {
+        auto shoup_q = [](uint64_t w, uint64_t q) { return (uint64_t)(((unsigned __int128)w << 64) / q); };
+        CrtArgs64Fast f{};
+        f.t = nprimes;
+        f.p = p;
+        f.mp = ~0ull / p;
+        for (int j = 0; j < nprimes; j++) {
+            const uint64_t qj = primes[j];
+            f.q[j] = qj;
+            f.mq[j] = ~0ull / qj;
+            f.ginv[j] = a.ginv[j] % qj;
+            f.ginvs[j] = shoup_q(f.ginv[j], qj);
+            for (int l = 0; l < j; l++) {
+                f.qlj[l][j] = primes[l] % qj;
+                f.qljs[l][j] = shoup_q(f.qlj[l][j], qj);
+            }
+            f.qlp[j] = qj % p;
+            f.qlps[j] = shoup_q(f.qlp[j], p);
+        }
+        multimod_crt_fast_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, f);
+    } else {
+        multimod_crt_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, a);
+    }
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());

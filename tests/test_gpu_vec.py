@@ -137,3 +137,23 @@ def test_dot_multi_column_pairs(ctx, ln, k, off):
     uv = pml_gb300.nmod_vec_dot_product_multi(to_dev(u), dv, q, ctx=ctx)
     ref = [oracle.nmod_vec_dot(u, np.ascontiguousarray(v[:, j]), q) for j in range(k)]
     assert list(uv.cpu().numpy().view(np.uint64)) == ref
+
+
+@pytest.mark.parametrize("primes,p", [
+    ([9223372036854775783, 9223372036854775643, 9223372036854775549, 9223372036854775507], 9223372036854775783),
+    ([9223372036854775783, 9223372036854775643, 9223372036854775549], 18446744073709551557),
+    ([659706976665601, 910395627798529, 1086317488242689, 1108307720798209], 2 ** 61 - 1),
+    ([9223372036854775783], 2),
+    ([1000003, 1000033, 1000037, 1000039, 1000081, 1000099], 9223372036854775807)])
+def test_multimod_crt_bounds(ctx, primes, p):
+    """CRT back mod p with primes just below 2^63 (the largest Barrett remainders and
+    Shoup products), p just below and above 2^63 (the 64-bit and the 128-bit kernels),
+    six primes, residues all q_j - 1 and random."""
+    import pml_gb300
+    rng = np.random.default_rng(len(primes) + p % 1000)
+    nb = 5000
+    res = np.stack([rng.integers(0, q, nb, dtype=np.uint64) for q in primes])
+    res[:, 0] = [q - 1 for q in primes]
+    res[:, 1] = 0
+    out = pml_gb300.nmod_multimod_CRT_CRT(to_dev(res), primes, p, ctx=ctx)
+    assert np.array_equal(out.cpu().numpy().view(np.uint64), oracle.multimod_crt(res, primes, p))
