@@ -385,16 +385,20 @@ __device__ __forceinline__ uint64_t shoup64(uint64_t v, uint64_t w, uint64_t ws,
     return r >= q ? r - q : r;
 }
 
+// T primes, a compile-time count: the digits c[] stay in registers
+template <int T>
 __global__ void multimod_crt_fast_kernel(uint64_t *out, const uint64_t *__restrict__ res, int64_t nb,
                                          CrtArgs64Fast a)
 {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nb; i += (int64_t)gridDim.x * blockDim.x) {
-        uint64_t c[kMaxPrimes];
+        uint64_t c[T];
         c[0] = red64(res[i], a.q[0], a.mq[0]);
-        for (int j = 1; j < a.t; j++) {
+#pragma unroll
+        for (int j = 1; j < T; j++) {
             const uint64_t qj = a.q[j], mj = a.mq[j];
             // c_0 + c_1 q_0 + ... + c_{j-1} q_0 ... q_{j-2} mod q_j, by Horner from the top
             uint64_t v = red64(c[j - 1], qj, mj);
+#pragma unroll
             for (int l = j - 2; l >= 0; l--) {
                 v = shoup64(v, a.qlj[l][j], a.qljs[l][j], qj) + red64(c[l], qj, mj);
                 v = v >= qj ? v - qj : v;
@@ -403,8 +407,9 @@ __global__ void multimod_crt_fast_kernel(uint64_t *out, const uint64_t *__restri
             const uint64_t d = r >= v ? r - v : r + (qj - v);
             c[j] = shoup64(d, a.ginv[j], a.ginvs[j], qj);
         }
-        uint64_t x = red64(c[a.t - 1], a.p, a.mp);
-        for (int l = a.t - 2; l >= 0; l--) {
+        uint64_t x = red64(c[T - 1], a.p, a.mp);
+#pragma unroll
+        for (int l = T - 2; l >= 0; l--) {
             x = shoup64(x, a.qlp[l], a.qlps[l], a.p) + red64(c[l], a.p, a.mp);
             x = x >= a.p ? x - a.p : x;
         }
@@ -665,7 +670,15 @@ PMLG_API int pmlg_multimod_crt(pmlg_ctx *ctx, uint64_t *out, const uint64_t *res
             f.qlp[j] = qj % p;
             f.qlps[j] = shoup_q(f.qlp[j], p);
         }
-        multimod_crt_fast_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, f);
+        const int g = grid_for(ctx, nb, 256, 8);
+        switch (nprimes) {
+        case 1: multimod_crt_fast_kernel<1><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        case 2: multimod_crt_fast_kernel<2><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        case 3: multimod_crt_fast_kernel<3><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        case 4: multimod_crt_fast_kernel<4><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        case 5: multimod_crt_fast_kernel<5><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        default: multimod_crt_fast_kernel<6><<<g, 256, 0, st>>>(out, residues, nb, f); break;
+        }
     } else {
         multimod_crt_kernel<<<grid_for(ctx, nb, 256, 8), 256, 0, st>>>(out, residues, nb, a);
     }
