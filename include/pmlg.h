@@ -93,7 +93,8 @@ PMLG_API int pmlg_ctx_set_tuning(pmlg_ctx *ctx, int on);
  * -PMLG_EINVAL for a shape outside 1..64 */
 PMLG_API int pmlg_ctx_tuned_form(const pmlg_ctx *ctx, int r, int k, int c, int64_t npts);
 /* pmlg_poly_mat_mul_batch: on (the default), a batch called again with the same jobs is
- * captured into a CUDA graph on its second call and replayed on later ones */
+ * captured into a CUDA graph on its second call and replayed on later ones; a capture that
+ * fails falls back to direct launches and leaves replay off until this is called again */
 PMLG_API int pmlg_ctx_set_batch_graphs(pmlg_ctx *ctx, int on);
 /* pmbasis leaf order (mbasis below it); 0 restores the tuned default */
 PMLG_API int pmlg_ctx_set_leaf_order(pmlg_ctx *ctx, int64_t order);

@@ -645,7 +645,8 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
     const unsigned long long recorded = ctx->launches - l0;   // kernels the capture recorded
     ctx->launches = l0;
     if (s != PMLG_OK || !exec) {
-        // the capture failed: clear its error and launch directly
+        // the capture failed: clear its error, launch directly, and leave graphs off for
+        // this context (pmlg_ctx_set_batch_graphs turns them back on)
         (void)cudaGetLastError();
         if (exec) cudaGraphExecDestroy(exec);
         ctx->batch_graphs = 0;
