@@ -134,3 +134,38 @@ def test_find_root_and_primes():
     assert oracle.is_prime(P998) and not oracle.is_prime(P998 + 2)
     q = oracle.rand_prime(59, 7)
     assert q.bit_length() == 59 and oracle.is_prime(q)
+
+
+@pytest.mark.parametrize("primes,p", [
+    ([9223372036854775783, 9223372036854775643, 9223372036854775549, 9223372036854775507], 9223372036854775783),
+    ([9223372036854775783, 9223372036854775643, 9223372036854775549], 18446744073709551557),
+    ([1000003, 1000033, 1000037, 1000039, 1000081, 1000099], 9223372036854775807),
+    ([9223372036854775783], 2)])
+def test_multimod_oracle_against_big_integers(primes, p):
+    """The oracle's multimodular reduction and CRT (the checker of the GPU kernels at
+    primes just below 2^63 and p on both sides of 2^63) against Python big integers."""
+    from math import prod
+    rng = np.random.default_rng(len(primes))
+    nb = 200
+    res = np.stack([rng.integers(0, q, nb, dtype=np.uint64) for q in primes])
+    res[:, 0] = [q - 1 for q in primes]
+    out = oracle.multimod_crt(res, primes, p)
+    M = prod(primes)
+    for i in range(nb):
+        x = 0
+        for j, q in enumerate(primes):
+            Mj = M // q
+            x += int(res[j, i]) * Mj * pow(Mj, -1, q)
+        assert int(out[i]) == (x % M) % p
+    x = rng.integers(0, 2 ** 63, nb, dtype=np.uint64)
+    red = oracle.multimod_reduce(x, primes)
+    assert all(int(red[j, i]) == int(x[i]) % q for j, q in enumerate(primes) for i in range(nb))
+
+
+def test_dot_oracle_against_big_integers():
+    """The oracle's dot products at the largest entries (all p - 1, 64- and 32-bit) against
+    Python big integers."""
+    for p, n in [(2 ** 63 - 25, 5000), (2 ** 64 - 59, 3000), (4294967291, 7000)]:
+        a = np.full(n, p - 1, dtype=np.uint64)
+        b = np.random.default_rng(n).integers(0, p, n, dtype=np.uint64)
+        assert oracle.nmod_vec_dot(a, b, p) == sum(int(u) * int(v) for u, v in zip(a, b)) % p
