@@ -138,6 +138,37 @@ def make_inputs(seed: int):
     return A, B
 
 
+def pointwise_batch_inputs(seed: int):
+    """The pointwise contraction alone: 4096 pairs of 64x64 matrices, uint32 entries
+    uniform in [0, p) (numpy PCG64)."""
+    rng = np.random.default_rng(seed)
+    A = rng.integers(0, P, size=(4096, 64, 64), dtype=np.uint32)
+    B = rng.integers(0, P, size=(4096, 64, 64), dtype=np.uint32)
+    return A, B
+
+
+def pmbasis_input(seed: int):
+    """pmbasis input: a 64x32 matrix of length 8192 (the order), coefficients uniform in [0, p)."""
+    rng = np.random.default_rng(seed)
+    return rng.integers(0, P, size=(PM_M, PM_N, PM_ORDER), dtype=np.uint64)
+
+
+def uneven_instances(seed: int):
+    """The batched uneven workload: 256 products A_i B_i of square m_i x m_i matrices,
+    m_i uniform in {4..48}, lengths 2^U(6,12), even i mod p = 998244353, odd i mod a
+    seeded random 59-bit prime; coefficients uniform in [0, p_i)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(256):
+        m = int(rng.integers(4, 49))
+        ln = int(2 ** rng.uniform(6, 12))
+        p = P if i % 2 == 0 else random_prime(59, rng)
+        A = rng.integers(0, p, size=(m, m, ln), dtype=np.uint64)
+        B = rng.integers(0, p, size=(m, m, ln), dtype=np.uint64)
+        out.append((A, B, p))
+    return out
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -336,9 +367,9 @@ def measure_pointwise_batch(ctx, dev, st, forms, rank):
     import torch
     import pml_gb300
     nb = 4096
-    rng = np.random.default_rng(11 + rank)
-    A = torch.from_numpy(rng.integers(0, P, size=(nb, 64, 64), dtype=np.uint32).view(np.int32)).to(dev)
-    B = torch.from_numpy(rng.integers(0, P, size=(nb, 64, 64), dtype=np.uint32).view(np.int32)).to(dev)
+    hA, hB = pointwise_batch_inputs(11 + rank)
+    A = torch.from_numpy(hA.view(np.int32)).to(dev)
+    B = torch.from_numpy(hB.view(np.int32)).to(dev)
     res, outs = {}, {}
     for name, form in forms:
         ctx.set_form(form)
@@ -357,14 +388,11 @@ def measure_batched_uneven(ctx, dev, st, forms, rank):
     sizes m uniform in {4..48}, lengths 2^U(6,12), half p = 998244353, half seeded 59-bit primes."""
     import torch
     import pml_gb300
-    rng = np.random.default_rng(5 + rank)
     jobs, macs = [], 0
-    for i in range(256):
-        m = int(rng.integers(4, 49))
-        ln = int(2 ** rng.uniform(6, 12))
-        p = P if i % 2 == 0 else random_prime(59, rng)
-        A = torch.from_numpy(rng.integers(0, p, size=(m, m, ln), dtype=np.uint64).view(np.int64)).to(dev)
-        B = torch.from_numpy(rng.integers(0, p, size=(m, m, ln), dtype=np.uint64).view(np.int64)).to(dev)
+    for hA, hB, p in uneven_instances(5 + rank):
+        m, ln = hA.shape[0], hA.shape[2]
+        A = torch.from_numpy(hA.view(np.int64)).to(dev)
+        B = torch.from_numpy(hB.view(np.int64)).to(dev)
         jobs.append((A, B, p))
         macs += m ** 3 * ln
     res, outs = {}, {}
@@ -699,8 +727,7 @@ def run_pml(args):
     # pmbasis 64x32, order 8192, every form (one warm-up call, then the median of three timed calls)
     pm = None
     if not args.no_pmbasis:
-        rng = np.random.default_rng(7 + rank)
-        F = rng.integers(0, P, size=(PM_M, PM_N, PM_ORDER), dtype=np.uint64)
+        F = pmbasis_input(7 + rank)
         dF = torch.from_numpy(F.view(np.int64)).to(dev)
         pm = {}
         outs = {}

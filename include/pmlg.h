@@ -199,7 +199,9 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
  * shift `shift` (host, m entries; in: input shift, out: shifted row degree).
  * appbas: device, m x m of capacity appbas_cap >= order + 1 (fully written).
  * *appbas_len (host, may be NULL) receives the max length of appbas.
- * p must be a prime < 2^30.  The stream is synchronised before return.
+ * p must be a prime (any word size, 2 <= p < 2^64); m, n <= 1024.  The leaves run on
+ * 32-bit residues for p < 2^30 and m, n <= 64, on 64-bit residues otherwise.  The
+ * stream is synchronised before return.
  * pmlg_pmbasis replaces nmod_poly_mat_pmbasis
  * (flint-extras/src/nmod_poly_mat_extra/approximant_basis.c:33-69);
  * pmlg_mbasis replaces nmod_poly_mat_mbasis (approximant_basis.c:18-31,
@@ -232,7 +234,7 @@ PMLG_API int pmlg_pmbasis_host(pmlg_ctx *ctx, uint64_t *appbas, int64_t appbas_c
  * [0, *nullity) receive the basis, in s-ordered weak Popov form, the other rows
  * are zero.  *ker_len receives the basis' max length (at least 1); when it is
  * above ker_cap, PMLG_ELEN is returned and nothing is written, so the caller can
- * retry with a larger buffer.  m <= 64, p a prime < 2^30.  The stream is
+ * retry with a larger buffer.  m <= 1024, p any word-size prime.  The stream is
  * synchronised before return.
  * Replaces nmod_poly_mat_kernel_zls_approx
  * (flint-extras/src/nmod_poly_mat_extra/kernel.c:232-480), and
@@ -265,7 +267,7 @@ PMLG_API int pmlg_kernel_zls_host(pmlg_ctx *ctx, uint64_t *ker, int64_t ker_cap,
 /* Truncated inverse: S (device, n x n of capacity order + 1) = A^-1 mod x^order for
  * A (device, n x n, entry stride alen), from the approximant basis of [A \\ -I] at
  * order with shift [0, ..., 0, order, ..., order].  *invertible = 1 when A(0) is
- * invertible (S written), 0 otherwise.  n <= 32, p a prime < 2^30; the stream is
+ * invertible (S written), 0 otherwise.  n <= 512, p any word-size prime; the stream is
  * synchronised.  Replaces nmod_poly_mat_inv_trunc
  * (flint-extras/src/nmod_poly_mat_extra/nmod_poly_mat_dixon.c:32-80). */
 PMLG_API int pmlg_inv_trunc(pmlg_ctx *ctx, uint64_t *S, const uint64_t *A, int64_t n, int64_t alen,
@@ -337,8 +339,10 @@ PMLG_API int pmlg_nmod_vec_dot_multi(pmlg_ctx *ctx, uint64_t *uv, const uint64_t
  * pmlg_nmod_vec_dot_multi, on the current device.
  * - k may be at most 65536; larger k returns PMLG_EUNSUP and nothing runs.
  * - The first call on a device looks up the array's device address
- *   (cudaGetSymbolAddress) with that device current.  Make that first call
- *   before any stream capture.
+ *   (cudaGetSymbolAddress) with that device current, and keeps it for the rest
+ *   of the process.  Make that first call before any stream capture, and do
+ *   not use this entry point across a cudaDeviceReset (the kept address would
+ *   then be stale).
  * - Every call shares the one array.  Calls that overlap on the GPU (on
  *   different streams, or from different threads) race on it and must be
  *   serialised by the caller.  No state carries over from one call to the

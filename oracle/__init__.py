@@ -48,6 +48,8 @@ def lib():
                                                 C.c_int64, C.c_int64, C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
             "orc_poly_mat_mul_ntt": (C.c_int, [_u64p, _u64p, _u64p, C.c_int64, C.c_int64, C.c_int64,
                                                C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
+            "orc_poly_mat_mul_crt": (C.c_int, [_u64p, _u64p, _u64p, C.c_int64, C.c_int64, C.c_int64,
+                                               C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
             "orc_mbasis": (C.c_int64, [_u64p, _i64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
                                        C.c_uint64]),
             "orc_pmbasis": (C.c_int64, [_u64p, _i64p, _u64p, C.c_int64, C.c_int64, C.c_int64, C.c_int64,
@@ -55,6 +57,7 @@ def lib():
             "orc_is_approximant_basis": (C.c_int, [_u64p, C.c_int64, _u64p, C.c_int64, C.c_int64, C.c_int64,
                                                    C.c_int64, _i64p, C.c_uint64]),
             "orc_nmod_vec_dot": (C.c_uint64, [_u64p, _u64p, C.c_int64, C.c_uint64]),
+            "orc_nmod_vec_dot_multi": (None, [_u64p, _u64p, _u64p, C.c_int64, C.c_int64, C.c_uint64, C.c_int]),
             "orc_nmod32_vec_dot": (C.c_uint32, [_u32p, _u32p, C.c_int64, C.c_uint64]),
             "orc_integer_dot": (None, [_u64p, _u64p, _u64p, C.c_int64]),
             "orc_nmod32_vec_mdot": (None, [_u32p, _u32p, _u32p, C.c_int64, C.c_int64, C.c_int64, C.c_uint64]),
@@ -203,6 +206,30 @@ def poly_mat_mul_ntt(A: np.ndarray, B: np.ndarray, p: int, nthreads: int = 1) ->
     if rc != 0:
         raise ValueError("modulus/length not supported by the NTT port")
     return out
+
+
+def poly_mat_mul_crt(A: np.ndarray, B: np.ndarray, p: int, nthreads: int = 1) -> np.ndarray:
+    """A * B mod any p >= 2 through NTT products modulo up to six primes below 2^30 and
+    Garner's CRT (the fast oracle product for moduli that are not NTT primes)."""
+    A, B = _c64(A), _c64(B)
+    r, k, l1 = A.shape
+    _, c, l2 = B.shape
+    if l1 == 0 or l2 == 0:
+        return np.zeros((r, c, 0), dtype=np.uint64)
+    out = np.empty((r, c, l1 + l2 - 1), dtype=np.uint64)
+    rc = lib().orc_poly_mat_mul_crt(_p64(out), _p64(A), _p64(B), r, k, c, l1, l2, p, nthreads)
+    if rc != 0:
+        raise ValueError("product beyond the multi-prime oracle's bound")
+    return out
+
+
+def poly_mat_mul_fast(A: np.ndarray, B: np.ndarray, p: int, nthreads: int = 1) -> np.ndarray:
+    """The fastest oracle product for the modulus: the single-prime NTT port when p is an
+    NTT prime of the transform length, else the multi-prime product."""
+    try:
+        return poly_mat_mul_ntt(A, B, p, nthreads=nthreads)
+    except ValueError:
+        return poly_mat_mul_crt(A, B, p, nthreads=nthreads)
 
 
 def poly_mat_mulmid(A: np.ndarray, B: np.ndarray, nlo: int, nhi: int, p: int, nthreads: int = 1):
@@ -416,6 +443,16 @@ def mat_poly_to_poly_mat(M: np.ndarray, order: int, out_cap: int = None):
 def nmod_vec_dot(v1: np.ndarray, v2: np.ndarray, p: int) -> int:
     v1, v2 = _c64(v1), _c64(v2)
     return int(lib().orc_nmod_vec_dot(_p64(v1), _p64(v2), len(v1), p))
+
+
+def nmod_vec_dot_multi(u: np.ndarray, v: np.ndarray, p: int, nthreads: int = 1) -> np.ndarray:
+    """uv[j] = sum_i u[i] v[i, j] mod p for v of shape (len, k)."""
+    u = _c64(u)
+    v = _c64(v)
+    ln, k = v.shape
+    out = np.empty(k, dtype=np.uint64)
+    lib().orc_nmod_vec_dot_multi(_p64(out), _p64(u), _p64(v), ln, k, p, nthreads)
+    return out
 
 
 def nmod32_vec_dot(v1: np.ndarray, v2: np.ndarray, p: int) -> int:

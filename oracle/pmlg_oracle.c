@@ -562,20 +562,17 @@ static void cpu_ntt_inv(const cpu_ntt_t *T, uint32_t *a)
     }
 }
 
-int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
-                         int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
-                         uint64_t p, int nthreads)
+/* residues mod q (an NTT prime < 2^30 with N | q - 1) of the coefficients [0, len) of
+ * A * B, entry-major with entry stride len; inputs are reduced mod q as they are read */
+static int ntt_product_mod_q(uint32_t *out, const uint64_t *A, const uint64_t *B,
+                             int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                             uint32_t q, int nthreads)
 {
-    (void) nthreads;
-    if (len1 <= 0 || len2 <= 0)
-        return 0;
-    if (p >= (1ULL << 30))
-        return -1;
     const int64_t len = len1 + len2 - 1;
     int64_t N = 1;
     while (N < len) N <<= 1;
     cpu_ntt_t T;
-    if (cpu_ntt_init(&T, (uint32_t) p, N) != 0)
+    if (cpu_ntt_init(&T, q, N) != 0)
         return -1;
     /* point-major evaluations: E[pt][i][j] */
     uint32_t *EA = (uint32_t *) malloc(sizeof(uint32_t) * (size_t) (N * r * k));
@@ -598,7 +595,7 @@ int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
             const uint64_t *src = isA ? A + ee * len1 : B + ee * len2;
             const int64_t L = isA ? len1 : len2;
             for (int64_t d = 0; d < N; d++)
-                buf[d] = d < L ? (uint32_t) src[d] : 0;
+                buf[d] = d < L ? (uint32_t) (src[d] >= q ? src[d] % q : src[d]) : 0;
             cpu_ntt_fwd(&T, buf);
             uint32_t *dst = isA ? EA : EB;
             const int64_t stride = isA ? r * k : k * c;
@@ -629,7 +626,7 @@ int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
                         lo += (uint64_t) a[i * k + l] * b[l * c + j];
                     hi += lo >> 32;
                     lo &= 0xffffffffULL;
-                    o[i * c + j] = (uint32_t) ((((u128) hi << 32) + lo) % p);
+                    o[i * c + j] = (uint32_t) ((((u128) hi << 32) + lo) % q);
                 }
         }
 #ifdef _OPENMP
@@ -641,12 +638,137 @@ int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
                 buf[d] = EC[d * r * c + e];
             cpu_ntt_inv(&T, buf);
             for (int64_t d = 0; d < len; d++)
-                C[e * len + d] = buf[d];
+                out[e * len + d] = buf[d];
         }
         free(buf);
     }
     free(EA); free(EB); free(EC);
     cpu_ntt_clear(&T);
+    return 0;
+}
+
+int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
+                         int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                         uint64_t p, int nthreads)
+{
+    if (len1 <= 0 || len2 <= 0)
+        return 0;
+    if (p >= (1ULL << 30))
+        return -1;
+    const int64_t len = len1 + len2 - 1;
+    uint32_t *R = (uint32_t *) malloc(sizeof(uint32_t) * (size_t) (r * c * len + 1));
+    const int rc = ntt_product_mod_q(R, A, B, r, k, c, len1, len2, (uint32_t) p, nthreads);
+    if (rc == 0)
+        for (int64_t i = 0; i < r * c * len; i++)
+            C[i] = R[i];
+    free(R);
+    return rc;
+}
+
+/* ------------------------------------------------------------------ */
+/* multi-prime product for any modulus                                 */
+/* ------------------------------------------------------------------ */
+
+/* The NTT primes of the multi-prime product: the largest q = a 2^20 + 1 < 2^30 that are
+ * prime, found by a downward search over a (each q > 2^29, transforms up to 2^20). */
+#define ORC_CRT_MAXT 6
+static uint32_t crt_q[ORC_CRT_MAXT];
+static int crt_nq = 0;
+
+static void crt_primes_init(void)
+{
+    if (crt_nq == ORC_CRT_MAXT)
+        return;
+    int n = 0;
+    uint32_t found[ORC_CRT_MAXT];
+    for (uint64_t a = 1023; a >= 512 && n < ORC_CRT_MAXT; a--)
+    {
+        const uint64_t q = (a << 20) + 1;
+        if (orc_is_prime(q))
+            found[n++] = (uint32_t) q;
+    }
+    for (int i = 0; i < n; i++)
+        crt_q[i] = found[i];
+    crt_nq = n;
+}
+
+static int bits_of(uint64_t x)
+{
+    int b = 0;
+    while (x) { b++; x >>= 1; }
+    return b;
+}
+
+/*
+ * C = A * B mod p for any p >= 2: the exact integer product (entries below
+ * k * min(len1, len2) * (p-1)^2) modulo t NTT primes, recombined by Garner's mixed
+ * radix form and reduced mod p.  This is the multi-prime design of the reference's
+ * disabled product (nmod_poly_mat_mul_3_primes.bak:59-153: the prime count from
+ * 2 bits(p) + bits(k) + bits(min len)), with primes below 2^30.  Returns -1 when the
+ * bound needs more than ORC_CRT_MAXT primes or the transform exceeds 2^20.
+ */
+int orc_poly_mat_mul_crt(uint64_t *C, const uint64_t *A, const uint64_t *B,
+                         int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                         uint64_t p, int nthreads)
+{
+    if (len1 <= 0 || len2 <= 0)
+        return 0;
+    const int64_t len = len1 + len2 - 1;
+    if (len > (1LL << 20))
+        return -1;
+    crt_primes_init();
+    const int64_t minlen = len1 < len2 ? len1 : len2;
+    const int need = bits_of((uint64_t) k) + bits_of((uint64_t) minlen) + 2 * bits_of(p - 1);
+    int t = (need + 28) / 29;    /* every prime is > 2^29 */
+    if (t < 1) t = 1;
+    if (t > crt_nq)
+        return -1;
+    const int64_t nco = r * c * len;
+    uint32_t *R = (uint32_t *) malloc(sizeof(uint32_t) * (size_t) (t * nco + 1));
+    for (int j = 0; j < t; j++)
+        if (ntt_product_mod_q(R + j * nco, A, B, r, k, c, len1, len2, crt_q[j], nthreads) != 0)
+        {
+            free(R);
+            return -1;
+        }
+    /* inv[j] = (q_0 ... q_{j-1})^-1 mod q_j; qp[j] = q_0 ... q_{j-1} mod p */
+    uint64_t inv[ORC_CRT_MAXT], qp[ORC_CRT_MAXT];
+    qp[0] = 1 % p;
+    inv[0] = 1;
+    for (int j = 1; j < t; j++)
+    {
+        uint64_t pr = 1;
+        for (int l = 0; l < j; l++)
+            pr = orc_mulmod(pr, crt_q[l] % crt_q[j], crt_q[j]);
+        inv[j] = orc_invmod(pr, crt_q[j]);
+        qp[j] = orc_mulmod(qp[j - 1], crt_q[j - 1] % p, p);
+    }
+    const int nt = nthreads > 0 ? nthreads : 1;
+    (void) nt;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nt)
+#endif
+    for (int64_t i = 0; i < nco; i++)
+    {
+        uint64_t v[ORC_CRT_MAXT];
+        v[0] = R[i];
+        for (int j = 1; j < t; j++)
+        {
+            const uint64_t qj = crt_q[j];
+            /* (v_0 + v_1 q_0 + ... + v_{j-1} q_0..q_{j-2}) mod q_j by Horner */
+            uint64_t acc = v[j - 1] % qj;
+            for (int l = j - 2; l >= 0; l--)
+                acc = (orc_mulmod(acc, crt_q[l], qj) + v[l]) % qj;
+            const uint64_t rj = R[j * nco + i];
+            v[j] = orc_mulmod((rj + qj - acc) % qj, inv[j], qj);
+        }
+        /* x = sum_j v_j (q_0 .. q_{j-1}) mod p */
+        uint64_t x = 0;
+        for (int j = 0; j < t; j++)
+            x = addmod(x, orc_mulmod(v[j] % p, qp[j], p), p);
+        C[i] = x;
+    }
+    free(R);
     return 0;
 }
 
@@ -658,7 +780,8 @@ static void pm_mul_auto(uint64_t *C, const uint64_t *A, const uint64_t *B,
     if (len1 <= 0 || len2 <= 0)
         return;
     if ((int64_t) r * k * c * len1 * len2 > (1LL << 22)
-        && orc_poly_mat_mul_ntt(C, A, B, r, k, c, len1, len2, p, nthreads) == 0)
+        && (orc_poly_mat_mul_ntt(C, A, B, r, k, c, len1, len2, p, nthreads) == 0
+            || orc_poly_mat_mul_crt(C, A, B, r, k, c, len1, len2, p, nthreads) == 0))
         return;
     orc_poly_mat_mul(C, A, B, r, k, c, len1, len2, p, nthreads);
 }
@@ -977,7 +1100,7 @@ int orc_is_approximant_basis(const uint64_t *appbas, int64_t alen,
     /* residual = appbas * F; coefficients below order must vanish */
     const int64_t rl = alen + flen - 1;
     uint64_t *resid = (uint64_t *) malloc(sizeof(uint64_t) * (size_t) (m * n * rl));
-    orc_poly_mat_mul(resid, appbas, F, m, m, n, alen, flen, p, 1);
+    pm_mul_auto(resid, appbas, F, m, m, n, alen, flen, p, 1);
     for (int64_t e = 0; e < m * n && !(fail & 2); e++)
         for (int64_t t = 0; t < order && t < rl; t++)
             if (resid[e * rl + t]) { fail |= 2; break; }
@@ -1071,6 +1194,35 @@ uint64_t orc_nmod_vec_dot(const uint64_t *v1, const uint64_t *v2, int64_t len, u
     acc = ((acc << 64) | r[1]) % p;
     acc = ((acc << 64) | r[0]) % p;
     return (uint64_t) acc;
+}
+
+/* uv[j] = sum_{i<len} u[i] v[i*k + j] mod p, j < k (nmod_vec_dot_product_multi,
+ * nmod_vec_dot_product_multi.c:2054, with the rows of v contiguous): every column an
+ * exact 192-bit sum reduced once, columns in parallel */
+void orc_nmod_vec_dot_multi(uint64_t *uv, const uint64_t *u, const uint64_t *v, int64_t len, int64_t k,
+                            uint64_t p, int nthreads)
+{
+    (void) nthreads;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+    for (int64_t j = 0; j < k; j++)
+    {
+        uint64_t r0 = 0, r1 = 0, r2 = 0;
+        for (int64_t i = 0; i < len; i++)
+        {
+            const u128 t = (u128) u[i] * v[i * k + j];
+            const uint64_t lo = (uint64_t) t, hi = (uint64_t) (t >> 64);
+            r0 += lo;
+            const uint64_t h = hi + (r0 < lo);   /* hi <= 2^64 - 2: no wrap */
+            r1 += h;
+            r2 += r1 < h;
+        }
+        u128 acc = r2 % p;
+        acc = ((acc << 64) | r1) % p;
+        acc = ((acc << 64) | r0) % p;
+        uv[j] = (uint64_t) acc;
+    }
 }
 
 uint32_t orc_nmod32_vec_dot(const uint32_t *v1, const uint32_t *v2, int64_t len, uint64_t p)

@@ -92,6 +92,12 @@ int64_t orc_poly_mat_mulmid(uint64_t *res, const uint64_t *A, const uint64_t *B,
 int orc_poly_mat_mul_ntt(uint64_t *C, const uint64_t *A, const uint64_t *B,
                          int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
                          uint64_t p, int nthreads);
+/* C = A * B mod any p >= 2 by NTT products modulo up to 6 primes below 2^30 and
+ * Garner's CRT (the multi-prime design of nmod_poly_mat_mul_3_primes.bak:59-153);
+ * -1 when the product needs more primes or a transform beyond 2^20. */
+int orc_poly_mat_mul_crt(uint64_t *C, const uint64_t *A, const uint64_t *B,
+                         int64_t r, int64_t k, int64_t c, int64_t len1, int64_t len2,
+                         uint64_t p, int nthreads);
 
 /* ---- approximant bases ---- */
 /* nmod_poly_mat_mbasis (approximant_basis.c:18-31 -> nmod_mat_poly_mbasis.c:116-378).
@@ -120,6 +126,8 @@ int orc_is_approximant_basis(const uint64_t *appbas, int64_t alen,
 /* sum v1[i]*v2[i] mod p for arbitrary 64-bit entries (not assumed reduced),
  * nmod_vec_dot_product_unbalanced, nmod_vec_dot_product.c:136-147 */
 uint64_t orc_nmod_vec_dot(const uint64_t *v1, const uint64_t *v2, int64_t len, uint64_t p);
+void orc_nmod_vec_dot_multi(uint64_t *uv, const uint64_t *u, const uint64_t *v, int64_t len, int64_t k,
+                            uint64_t p, int nthreads);
 /* 32-bit storage, _nmod32_vec_dot_split, nmod32_vec/dot_split.c:18-47 */
 uint32_t orc_nmod32_vec_dot(const uint32_t *v1, const uint32_t *v2, int64_t len, uint64_t p);
 /* exact integer dot product in 3 limbs, nmod_vec_integer_dot_product.c:13 */

@@ -19,7 +19,7 @@ LIB = PKG / "libpmlg.so"
 INCLUDE = PKG.parent / "include"
 
 SOURCES = ["context.cu", "ntt.cu", "pointwise.cu", "polymat.cu", "approx.cu", "vec.cu", "kernel.cu",
-           "layout.cu", "dixon.cu", "popov.cu"]
+           "layout.cu", "dixon.cu", "popov.cu", "leaf64.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
                      "-I", str(INCLUDE)]

@@ -19,6 +19,7 @@
 //      the nullity is 0, appbas *= x^(order-ord) (:221-231).
 #include "polymat.cuh"
 #include "ntt.cuh"
+#include "leaf64.cuh"
 
 #include <cooperative_groups.h>
 #include <vector>
@@ -852,15 +853,26 @@ struct Arena
     }
 };
 
-// bytes the recursion needs at order o (upper bound)
-static size_t pm_arena_bytes(int64_t m, int64_t n, int64_t o, int64_t leaf)
+// whether the leaves run on uint64 residues (leaf64.cu): primes from 2^30 up, or more
+// than 64 rows or columns
+static bool wide_leaf(int64_t m, int64_t n, uint64_t p)
 {
-    if (o <= leaf) return (size_t)(o * m * n + (o + 1) * m * m) * 4 + 1024;
+    return p >= (1ull << 30) || m > LEAF_MAX || n > LEAF_MAX;
+}
+
+// bytes the recursion needs at order o (upper bound)
+static size_t pm_arena_bytes(int64_t m, int64_t n, int64_t o, int64_t leaf, bool wide)
+{
+    if (o <= leaf) {
+        if (wide) return leaf64_scratch_bytes((int)m, (int)n, (int)o, nullptr, nullptr) + 1024;
+        return (size_t)(o * m * n + (o + 1) * m * m) * 4 + 1024;
+    }
     const int64_t o1 = o >> 1, o2 = o - o1;
     size_t here = (size_t)(m * m * (o1 + 1) + m * n * o2 + m * m * (o2 + 1)) * 8 + 1024;
-    size_t c1 = pm_arena_bytes(m, n, o1, leaf), c2 = pm_arena_bytes(m, n, o2, leaf);
+    size_t c1 = pm_arena_bytes(m, n, o1, leaf, wide), c2 = pm_arena_bytes(m, n, o2, leaf, wide);
     return here + (c1 > c2 ? c1 : c2);
 }
+
 
 struct PmState
 {
@@ -873,9 +885,36 @@ struct PmState
     unsigned long long *d_tmp;
 };
 
+// the uint64 leaf: scratch from the arena, one CTA
+static int leaf64_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, int64_t ldF, int64_t flen,
+                      int64_t order)
+{
+    const size_t mark = S.ar.top;
+    const int m = (int)S.m, n = (int)S.n, o = (int)order;
+    const int mn = m < n ? m : n;
+    bool e_sh = false, x_sh = false;
+    leaf64_scratch_bytes(m, n, o, &e_sh, &x_sh);
+    Leaf64Args a{};
+    a.R = (uint64_t *)S.ar.alloc((size_t)o * m * n * 8 + 8);
+    a.AB = (uint64_t *)S.ar.alloc((size_t)(o + 1) * m * m * 8);
+    a.E = e_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)n * m * 8);
+    a.X = x_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)m * mn * 8);
+    if (!a.R || !a.AB || (!e_sh && !a.E) || (!x_sh && !a.X)) return PMLG_ENOMEM;
+    a.F = F; a.ldF = ldF; a.flen = flen;
+    a.out = out; a.ldo = ldo;
+    a.shift = S.d_shift;
+    a.len_out = S.d_tmp;
+    a.m = m; a.n = n; a.order = o;
+    leaf64_set_modulus(a, S.p);
+    PMLG_TRY(leaf64_launch(S.ctx, a, S.st));
+    S.ar.top = mark;
+    return PMLG_OK;
+}
+
 static int leaf_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F, int64_t ldF, int64_t flen,
                     int64_t order)
 {
+    if (wide_leaf(S.m, S.n, S.p)) return leaf64_run(S, out, ldo, F, ldF, flen, order);
     const size_t mark = S.ar.top;
     uint32_t *R = (uint32_t *)S.ar.alloc((size_t)(order * S.m * S.n) * 4 + 4);
     uint32_t *AB = (uint32_t *)S.ar.alloc((size_t)((order + 1) * S.m * S.m) * 4);
@@ -1001,17 +1040,18 @@ static int approx_entry(pmlg_ctx *ctx, uint64_t *appbas, int64_t cap, int64_t *s
 {
     if (!ctx || !shift || m <= 0 || n <= 0 || flen < 0 || order < 0) return PMLG_EINVAL;
     if (cap < order + 1 || !appbas || (flen > 0 && !F)) return PMLG_EINVAL;
-    if (m > LEAF_MAX || n > LEAF_MAX) {
-        set_error(ctx, "approximant bases support m, n <= %d", LEAF_MAX);
+    if (m > LEAF64_MAXDIM || n > LEAF64_MAXDIM) {
+        set_error(ctx, "approximant bases support m, n <= %d", LEAF64_MAXDIM);
         return PMLG_EUNSUP;
     }
-    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
-        set_error(ctx, "approximant bases need a prime p < 2^30");
+    if (!h_is_prime(p)) {
+        set_error(ctx, "approximant bases need a prime modulus");
         return PMLG_EBADMOD;
     }
     PMLG_CUDA_TRY(cudaSetDevice(ctx->device));
     const int64_t leaf_eff = leaf < 1 ? 1 : leaf;
-    const size_t bytes = pm_arena_bytes(m, n, order > 0 ? order : 1, leaf_eff) + (size_t)m * 8 + 1024;
+    const size_t bytes =
+        pm_arena_bytes(m, n, order > 0 ? order : 1, leaf_eff, wide_leaf(m, n, p)) + (size_t)m * 8 + 1024;
     PMLG_TRY(ws_reserve(ctx, &ctx->ws_pm, bytes));
     PmState S{};
     S.ctx = ctx;

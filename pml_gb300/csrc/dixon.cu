@@ -13,6 +13,7 @@
 // (mul_geometric.c:32-119).  Every matrix stays in device memory.
 #include "pmlg_internal.cuh"
 #include "ntt.cuh"
+#include "leaf64.cuh"
 #include "polymat.cuh"
 
 #include <vector>
@@ -126,12 +127,12 @@ extern "C" PMLG_API int pmlg_inv_trunc(pmlg_ctx *ctx, uint64_t *S, const uint64_
 {
     if (!ctx || n < 0 || alen < 0 || order < 1 || !invertible) return PMLG_EINVAL;
     if (n > 0 && (!S || (alen > 0 && !A))) return PMLG_EINVAL;
-    if (2 * n > 64) {
-        set_error(ctx, "truncated inverses support n <= 32 (an approximant basis of 2n rows)");
+    if (2 * n > LEAF64_MAXDIM) {
+        set_error(ctx, "truncated inverses support n <= %d (an approximant basis of 2n rows)", LEAF64_MAXDIM / 2);
         return PMLG_EUNSUP;
     }
-    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
-        set_error(ctx, "truncated inverses need a prime p < 2^30");
+    if (!h_is_prime(p)) {
+        set_error(ctx, "truncated inverses need a prime modulus");
         return PMLG_EBADMOD;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -155,12 +156,12 @@ extern "C" PMLG_API int pmlg_dixon(pmlg_ctx *ctx, uint64_t *X, int64_t xcap, con
     const int64_t L = (sigma + order - 1) / order;
     if (xcap < L * order || xcap < 1) return PMLG_EINVAL;
     if (n > 0 && m > 0 && (!X || (alen > 0 && !A) || (blen > 0 && !B))) return PMLG_EINVAL;
-    if (2 * n > 64) {
-        set_error(ctx, "Dixon lifting supports n <= 32 (an approximant basis of 2n rows)");
+    if (2 * n > LEAF64_MAXDIM) {
+        set_error(ctx, "Dixon lifting supports n <= %d (an approximant basis of 2n rows)", LEAF64_MAXDIM / 2);
         return PMLG_EUNSUP;
     }
-    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
-        set_error(ctx, "Dixon lifting needs a prime p < 2^30");
+    if (!h_is_prime(p)) {
+        set_error(ctx, "Dixon lifting needs a prime modulus");
         return PMLG_EBADMOD;
     }
     cudaStream_t st = (cudaStream_t)stream;

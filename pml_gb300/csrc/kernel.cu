@@ -9,6 +9,7 @@
 // pmbasis returns.  Each step follows kernel.c line by line, so the output equals
 // the reference's for the same pmbasis and products, which are exact.
 #include "pmlg_internal.cuh"
+#include "leaf64.cuh"
 #include "polymat.cuh"
 
 #include <algorithm>
@@ -379,12 +380,12 @@ extern "C" PMLG_API int pmlg_kernel_zls(pmlg_ctx *ctx, uint64_t *ker, int64_t ke
     if (!ctx || m < 0 || n < 0 || plen < 0 || ker_cap < 1 || !nullity || !ker_len) return PMLG_EINVAL;
     if (m > 0 && (!ker || !pivind || !shift)) return PMLG_EINVAL;
     if (m > 0 && n > 0 && plen > 0 && !pmat) return PMLG_EINVAL;
-    if (m > 64) {
-        set_error(ctx, "kernel bases support m <= 64 (the approximant bases' limit)");
+    if (m > LEAF64_MAXDIM) {
+        set_error(ctx, "kernel bases support m <= %d (the approximant bases' limit)", LEAF64_MAXDIM);
         return PMLG_EUNSUP;
     }
-    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
-        set_error(ctx, "kernel bases need a prime p < 2^30");
+    if (!h_is_prime(p)) {
+        set_error(ctx, "kernel bases need a prime modulus");
         return PMLG_EBADMOD;
     }
     cudaStream_t st = (cudaStream_t)stream;
@@ -545,12 +546,12 @@ int64_t rank_mod_h(std::vector<uint64_t> a, int64_t r, int64_t c, uint64_t p)
 
 int check_kernel_args(pmlg_ctx *ctx, int64_t m, uint64_t p)
 {
-    if (m > 64) {
-        set_error(ctx, "kernel bases support m <= 64 (the approximant bases' limit)");
+    if (m > LEAF64_MAXDIM) {
+        set_error(ctx, "kernel bases support m <= %d (the approximant bases' limit)", LEAF64_MAXDIM);
         return PMLG_EUNSUP;
     }
-    if (p < 2 || p >= (1ull << 30) || !h_is_prime(p)) {
-        set_error(ctx, "kernel bases need a prime p < 2^30");
+    if (!h_is_prime(p)) {
+        set_error(ctx, "kernel bases need a prime modulus");
         return PMLG_EBADMOD;
     }
     return PMLG_OK;

@@ -157,6 +157,7 @@ struct pmlg_ctx
     struct BatchGraph
     {
         uint64_t key = 0;
+        std::vector<uint64_t> sig;           // the full batch description the key hashes
         cudaGraphExec_t exec = nullptr;
         unsigned long long launches = 0;
     };
@@ -165,6 +166,7 @@ struct pmlg_ctx
     BatchGraph bgraph[kBatchGraphs];
     int bgraph_next = 0;
     uint64_t batch_seen = 0;                 // key of the last batch launched directly
+    std::vector<uint64_t> batch_seen_sig;    // and its full description
 };
 
 namespace pmlg {

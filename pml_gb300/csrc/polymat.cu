@@ -606,8 +606,14 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     PMLG_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
     if (!ctx->batch_graphs || ctx->profiling || cs != cudaStreamCaptureStatusNone) return launch_all();
+    // the batch's full description (every pointer, shape and modulus, the form, the
+    // scratch and the stream) and its hash; a stored graph is replayed only when the
+    // whole description matches, not the hash alone
     uint64_t key = 1469598103934665603ull;
+    std::vector<uint64_t> sig;
+    sig.reserve(5 + 9 * (size_t)njobs);
     auto mix = [&](uint64_t v) {
+        sig.push_back(v);
         for (int b = 0; b < 8; b++) {
             key ^= (v >> (8 * b)) & 0xff;
             key *= 1099511628211ull;
@@ -622,13 +628,14 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
         mix(J.p);
     }
     for (auto &g : ctx->bgraph)
-        if (g.exec && g.key == key) {
+        if (g.exec && g.key == key && g.sig == sig) {
             PMLG_CUDA_TRY(cudaGraphLaunch(g.exec, st));
             count_launch(ctx, (unsigned)g.launches);
             return PMLG_OK;
         }
-    if (ctx->batch_seen != key) {
+    if (ctx->batch_seen != key || ctx->batch_seen_sig != sig) {
         ctx->batch_seen = key;
+        ctx->batch_seen_sig = sig;
         return launch_all();
     }
     // second call of this batch: capture, instantiate, launch
@@ -657,6 +664,7 @@ PMLG_API int pmlg_poly_mat_mul_batch(pmlg_ctx *ctx, const pmlg_polymat_job *jobs
     if (slotg.exec) cudaGraphExecDestroy(slotg.exec);
     slotg.exec = exec;
     slotg.key = key;
+    slotg.sig = std::move(sig);
     slotg.launches = recorded;
     PMLG_CUDA_TRY(cudaGraphLaunch(exec, st));
     count_launch(ctx, (unsigned)slotg.launches);

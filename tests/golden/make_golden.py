@@ -384,6 +384,18 @@ def main():
             assert is_approximant_basis(ab, F, order, shift, p), (p, m, n, order, fname)
             approx.append({"p": p, "m": m, "n": n, "order": order, "flen": flen, "seed": seed, "family": fname,
                            "shift_in": shift, "shift_out": sh, "appbas": ab})
+    # word-size primes of the reference's testing collection (40, 50 and 60 bits,
+    # testing_collection.h:16-20), a random 64-bit prime, and more than 64 rows
+    big = [(549755813911, 4, 2, 12, 12), (562949953421381, 5, 3, 10, 8), (576460752303423619, 3, 2, 9, 9),
+           (rand_prime(64, rng), 4, 3, 8, 8), (P998, 66, 2, 4, 4), (576460752303423619, 67, 3, 3, 3)]
+    for (p, m, n, order, flen) in big:
+        for fname, shift in shift_families(m, order, rng).items():
+            seed = 9500 + m * 13 + n + order
+            F = rand_pm(m, n, flen, p, seed)
+            ab, sh = mbasis(F, order, shift, p)
+            assert is_approximant_basis(ab, F, order, shift, p), (p, m, n, order, fname)
+            approx.append({"p": p, "m": m, "n": n, "order": order, "flen": flen, "seed": seed, "family": fname,
+                           "shift_in": shift, "shift_out": sh, "appbas": ab})
     # Pade-type input [[f], [-1]]: basis verified by the property check
     p = P998
     f = rand_vec(10, p, 4242)

@@ -127,6 +127,16 @@ def test_products_large_transforms(fctx, dims, p):
     assert np.array_equal(_mul(fctx, A, B, p), oracle.poly_mat_mul(A, B, p, nthreads=8))
 
 
+@pytest.mark.parametrize("dims", [(64, 64, 32, 4097, 8192), (64, 64, 64, 4096, 8192), (64, 32, 64, 8192, 4097)])
+def test_products_full_width_16384(fctx, dims):
+    """64-wide blocks at a transform of 16384 points, the shape of the check
+    appbas * F of a 64x32 pmbasis at order 8192: bit-exact against the oracle."""
+    r, k, c, l1, l2 = dims
+    A = oracle.rand_poly_mat(r, k, l1, P998, 41)
+    B = oracle.rand_poly_mat(k, c, l2, P998, 42)
+    assert np.array_equal(_mul(fctx, A, B, P998), oracle.poly_mat_mul_ntt(A, B, P998, nthreads=16))
+
+
 def test_products_config1_plain(fctx):
     """16x16 . 16x16, degree < 256, p = 998244353 (the CPU-runnable case)."""
     p = P998

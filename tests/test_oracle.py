@@ -98,6 +98,18 @@ def test_ntt_port_matches_schoolbook():
     assert np.array_equal(oracle.poly_mat_mul_ntt(A, B, p, nthreads=2), oracle.poly_mat_mul(A, B, p))
 
 
+@pytest.mark.parametrize("p", [2, 1000003, P998, 549755813911, 562949953421381, 576460752303423619,
+                               (1 << 63) - 25, (1 << 64) - 59])
+def test_crt_product_matches_schoolbook(p):
+    """The multi-prime product (NTT products modulo up to six primes below 2^30,
+    Garner's CRT) equals the schoolbook definition for moduli up to 2^64, with
+    all-(p-1) entries (the largest integer coefficients) and random ones."""
+    for (r, k, c, l1, l2, seed) in [(3, 4, 5, 17, 33, 1), (2, 7, 2, 60, 9, 2), (4, 3, 4, 33, 33, -1)]:
+        A = pm_from_seed(r, k, l1, p, seed)
+        B = pm_from_seed(k, c, l2, p, seed if seed == -1 else seed + 10)
+        assert np.array_equal(oracle.poly_mat_mul_crt(A, B, p, nthreads=2), oracle.poly_mat_mul(A, B, p))
+
+
 @pytest.mark.parametrize("seed", range(6))
 def test_pmbasis_reference_style(seed):
     """t-pmbasis.c:449-489 style: random prime, dims, order; verified basis,
@@ -169,3 +181,16 @@ def test_dot_oracle_against_big_integers():
         a = np.full(n, p - 1, dtype=np.uint64)
         b = np.random.default_rng(n).integers(0, p, n, dtype=np.uint64)
         assert oracle.nmod_vec_dot(a, b, p) == sum(int(u) * int(v) for u, v in zip(a, b)) % p
+
+
+@pytest.mark.parametrize("p", [P998, 2 ** 61 - 1, 18446744073709551557])
+def test_dot_multi_oracle_against_big_integers(p):
+    """The oracle's vector-matrix dot product (every column an exact sum, one
+    reduction) against Python big integers, random and all-(p-1) entries."""
+    u = oracle.rand_vec(257, p, 1)
+    v = oracle.rand_vec(257 * 9, p, 2).reshape(257, 9)
+    ref = [sum(int(a) * int(b) for a, b in zip(u, v[:, j])) % p for j in range(9)]
+    assert list(oracle.nmod_vec_dot_multi(u, v, p, nthreads=2)) == ref
+    u = np.full(4097, p - 1, dtype=np.uint64)
+    v = np.full((4097, 3), p - 1, dtype=np.uint64)
+    assert list(oracle.nmod_vec_dot_multi(u, v, p)) == [4097 * (p - 1) * (p - 1) % p] * 3
