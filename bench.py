@@ -247,6 +247,61 @@ def cpu_product_ms(nthreads: int, reps: int, warm: int):
     return statistics.median(t), t
 
 
+def _timed(fn):
+    t0 = time.perf_counter()
+    fn()
+    return (time.perf_counter() - t0) * 1e3
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def cpu_baselines():
+    """The oracle (C restatement of the reference's algorithms; FLINT/PML are not installed)
+    on the host cores for every workload of the benchmark set: 1 thread (the reference is
+    single-threaded) and all cores, each on a bounded sample stated beside it."""
+    import oracle
+    nt = os.cpu_count() or 1
+    res = {"cores_available": nt, "cpu": cpu_model(), "kind": "port"}
+    A1 = oracle.rand_poly_mat(16, 16, 256, P, 101)
+    B1 = oracle.rand_poly_mat(16, 16, 256, P, 102)
+    res["c1_product_16x16_len256"] = {"ms_1_thread": statistics.median(
+        [_timed(lambda: oracle.poly_mat_mul_ntt(A1, B1, P, nthreads=1)) for _ in range(5)]),
+        "sample": "full workload, median of 5"}
+    A2, B2 = pointwise_batch_inputs(11)
+    res["c2_pointwise_batch_4096"] = {
+        "ms_1_thread": _timed(lambda: oracle.nmod_mat_mul_batch_u32(A2, B2, P, nthreads=1)),
+        "ms_all_cores": _timed(lambda: oracle.nmod_mat_mul_batch_u32(A2, B2, P, nthreads=nt)),
+        "sample": "full workload (4096 products 64x64x64 mod p), one call each"}
+    A3, B3 = make_inputs(1)
+    res["c3_product_64x64_len4096"] = {
+        "ms_1_thread": _timed(lambda: oracle.poly_mat_mul_ntt(A3, B3, P, nthreads=1)),
+        "ms_all_cores": _timed(lambda: oracle.poly_mat_mul_ntt(A3, B3, P, nthreads=nt)),
+        "sample": "full workload, one call each"}
+    F = pmbasis_input(7)
+    res["c4_pmbasis_64x32_order8192"] = {
+        "ms_all_cores": _timed(lambda: oracle.pmbasis(F, PM_ORDER, [0] * PM_M, P, nthreads=nt)),
+        "ms_1_thread_order1024": _timed(lambda: oracle.pmbasis(F[:, :, :1024], 1024, [0] * PM_M, P, nthreads=1)),
+        "sample": "all cores: the full order-8192 call; 1 thread: the same input truncated to order 1024 "
+                  "(the 1-thread full call would take minutes)"}
+    inst = uneven_instances(5)
+    sub = inst[:64]
+    macs = lambda L: sum(A.shape[0] ** 3 * A.shape[2] for A, _, _ in L)
+    res["c5_batched_uneven_256"] = {
+        "ms_all_cores_first64": _timed(lambda: [oracle.poly_mat_mul_fast(A, B, p, nthreads=nt) for A, B, p in sub]),
+        "sample": f"the first 64 of the 256 instances ({macs(sub) / macs(inst):.3f} of the coefficient MACs), "
+                  "all cores; oracle products: single-prime NTT for p = 998244353, multi-prime NTT + CRT otherwise"}
+    return res
+
+
 def rank_barrier(world: int) -> None:
     """Barrier across the replicas (no-op for one process)."""
     if world > 1:
@@ -290,10 +345,12 @@ def run_reference(args):
 # GPU leg
 # ---------------------------------------------------------------------------
 
-# DRAM bytes (read + write) per launch of the dominant kernels at the headline workload, from one
-# ncu capture of `python bench.py --profile-case product` (profiles/ntt_kernels_n8192_4096polys.md,
-# profiles/pointwise_kernels_64x64_8192pts.md); a cold, single capture, so part of the output is
+# DRAM bytes (read + write) per launch of the dominant kernels at the headline workload: constants
+# from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of
+# `python bench.py --profile-case product`, a cold, single capture, so part of the output is
 # still in L2 when the kernel ends
+TRAFFIC_SOURCE = ("constant from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of "
+                  "`python bench.py --profile-case product`, not measured in this run")
 NCU_TRAFFIC = {"ntt_fwd": 217.1e6, "ntt_inv": 360.3e6, "pointwise_f16_tc": 368.2e6,
                "pointwise_int8_tc": 370.8e6, "pointwise_cuda_core": 367.1e6}
 
@@ -687,7 +744,7 @@ def run_pml(args):
             ach = work / avg_s / 1e9
             roofline = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s",
                         "frac": ach / peak, "traffic": NCU_TRAFFIC.get(dom),
-                        "traffic_unit": "bytes per launch (ncu)",
+                        "traffic_unit": "bytes per launch (ncu)", "traffic_source": TRAFFIC_SOURCE,
                         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                         "algorithmic_bytes_per_launch": work}
         else:
@@ -695,9 +752,26 @@ def run_pml(args):
             ach = work / avg_s / 1e12
             roofline = {"bound": "tensor", "kernel": dom, "achieved": ach, "peak": peak, "unit": "TFLOP/s",
                         "frac": ach / peak, "traffic": NCU_TRAFFIC.get(dom),
-                        "traffic_unit": "bytes per launch (ncu)",
+                        "traffic_unit": "bytes per launch (ncu)", "traffic_source": TRAFFIC_SOURCE,
                         "peak_source": "measured dense bf16 (burst)" if "bf16_tflops" in peaks else "fallback",
                         "algorithmic_ops_per_launch": work}
+
+    # the pointwise kernel beside it, against both of its roofs: FP16 digit-product rate against
+    # the dense bf16 peak, and its algorithmic bytes (A and B read, C written, uint32) against HBM
+    roofline_pw = None
+    if "pointwise_f16_tc" in prof_h:
+        pw_s = prof_h["pointwise_f16_tc"][0] / prof_h["pointwise_f16_tc"][1] / 1e3
+        flop = algorithmic_bytes("pointwise_f16_tc")[1]
+        pw_bytes = 3 * 8192 * R * C * 4
+        tpk = peaks.get("bf16_tflops", 1900.0)
+        hpk = peaks.get("hbm_gbs", 6800.0)
+        roofline_pw = {"kernel": "pointwise_f16_tc", "ms_per_launch": pw_s * 1e3,
+                       "tensor": {"achieved": flop / pw_s / 1e12, "peak": tpk, "unit": "TFLOP/s",
+                                  "frac": flop / pw_s / 1e12 / tpk,
+                                  "ops_per_launch": flop, "ops": "12 FP16 digit products per modular MAC x 2"},
+                       "hbm": {"achieved": pw_bytes / pw_s / 1e9, "peak": hpk, "unit": "GB/s",
+                               "frac": pw_bytes / pw_s / 1e9 / hpk, "algorithmic_bytes_per_launch": pw_bytes},
+                       "traffic": NCU_TRAFFIC.get("pointwise_f16_tc"), "traffic_source": TRAFFIC_SOURCE}
 
     # end to end through the host-buffer entry point, pinned host memory
     hA = torch.from_numpy(A.view(np.int64)).pin_memory()
@@ -757,6 +831,40 @@ def run_pml(args):
         pm["config"] = "pmbasis 64x32, order 8192, zero shift, p = 998244353, uniform coefficients"
         pm["timing"] = "median of three calls, wall clock around each (it synchronises internally), after one warm-up call"
 
+    # N > 1: the headline product row-sharded over the ranks (pml_gb300.shard): each rank
+    # transforms its rows of A and all of B, multiplies and interpolates its rows of C; the
+    # blocks of C are all-gathered over NCCL.  Strong scaling: one product in total.
+    sharded = None
+    if world > 1:
+        from pml_gb300.shard import poly_mat_mul_sharded, row_partition
+        ctx.set_form(HEAD)
+        for _ in range(args.warmup):
+            poly_mat_mul_sharded(dA, dB, P, ctx=ctx)
+        torch.cuda.synchronize()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            Cs = poly_mat_mul_sharded(dA, dB, P, ctx=ctx)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier()
+        sh_ms = ranks_max(e0.elapsed_time(e1) / args.steps)
+        e0.record(st)
+        for _ in range(args.steps):
+            poly_mat_mul_sharded(dA, dB, P, ctx=ctx, gather=False)
+        e1.record(st)
+        torch.cuda.synchronize()
+        barrier()
+        sh_ms_nog = ranks_max(e0.elapsed_time(e1) / args.steps)
+        step()
+        torch.cuda.synchronize()
+        sharded = {"ms_with_allgather": sh_ms, "ms_without_allgather": sh_ms_nog,
+                   "rows_per_rank": [b_ - a_ for a_, b_ in row_partition(R, world)],
+                   "matches_single_gpu": bool(torch.equal(Cs, dC)), "scaling": "strong",
+                   "config": "the headline product, rows of A and C split over the ranks, B transformed on "
+                             "every rank, C all-gathered (NCCL)"}
+
     # the two other GPU workloads of the benchmark set: the pointwise contraction alone and the
     # batched uneven products (every form, CUDA events around each call)
     extra = {} if args.no_extra else {
@@ -771,10 +879,12 @@ def run_pml(args):
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)
     cpu = None
+    cpu_all = None
     if rank == 0 and world == 1 and not args.no_cpu:
         med, ts = cpu_product_ms(1, 1, 0)
         cpu = {"value": med, "unit": "ms", "cores": 1, "kind": "port",
                "sample": "one full 64x64 len-4096 product, CPU evaluation/interpolation port (C, 1 thread)"}
+        cpu_all = cpu_baselines()
 
     if rank == 0:
         line = {
@@ -793,11 +903,14 @@ def run_pml(args):
                     "path": "pmlg_poly_mat_mul_host, pinned host buffers", "matches_device": e2e_ok},
             "gpu_launches": launches,
             "roofline": roofline,
+            "roofline_pointwise": roofline_pw,
             "kernels": {name: summarize(pr) for name, pr in profs.items()},
             "clocks": clocks,
             "pmbasis": pm,
             **extra,
             "cpu_baseline": cpu,
+            "cpu_baselines": cpu_all,
+            "row_sharded": sharded,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -470,6 +470,10 @@ ntt_inv_persist_kernel(NttInvArgs a)
 // The same, with the point tiles brought in by TMA tensor loads (256 tiles per
 // box, one transform = N / 1024 boxes) completing on an mbarrier; the wait is
 // bounded (on time-out the error word is set and the results are invalid).
+// Used up to N = 2^13 (32 KB per transform and mbarrier phase).  At N = 2^14,
+// where one phase expects 64 KB, this kernel returned wrong transforms for
+// about 0.5% of the entries of a 2048-entry launch on GB300, while the cp.async
+// kernel above was exact on the same inputs, so that size uses the cp.async one.
 template <int LG>
 __global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INVP_MIN)
 ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
@@ -477,6 +481,7 @@ ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
     extern __shared__ __align__(128) uint32_t smem[];
     constexpr int N = 1 << LG, NT = N / kPtTile, NBOX = NT / 256;
     constexpr uint32_t BYTES = (uint32_t)N * 4u;
+    static_assert(BYTES < 65536u, "one mbarrier phase expects less than 64 KB");
     uint32_t *x = smem;
     uint32_t *pf = smem + N + (N >> 4);                 // N + N/16 words: a multiple of 128 bytes
     __shared__ __align__(8) uint64_t bar;
@@ -611,8 +616,9 @@ static cudaError_t set_attrs()
         const int smp = (int)(((1 << LG) + (1 << (LG - 4)) + (1 << LG)) * sizeof(uint32_t));
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(ntt_inv_persist_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(ntt_inv_tma_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
+        if constexpr (LG <= 13)
+            if (e == cudaSuccess)
+                e = cudaFuncSetAttribute(ntt_inv_tma_kernel<LG>, cudaFuncAttributeMaxDynamicSharedMemorySize, smp);
     }
     return e;
 }
@@ -723,7 +729,7 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a0, cudaStream_t st)
         alignas(64) CUtensorMap tmap;
         std::memset(&tmap, 0, sizeof(tmap));
         bool tma = false;
-        if (PMLG_NTT_INV_TMA && a.nent <= 0x7fffffffll) {
+        if (PMLG_NTT_INV_TMA && a.lg <= 13 && a.nent <= 0x7fffffffll) {
             PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
             const cuuint64_t ntiles = (cuuint64_t)N / kPtTile * (cuuint64_t)a.t;
             const cuuint64_t gdim[3] = {(cuuint64_t)kPtTile, (cuuint64_t)a.nent, ntiles};
@@ -735,11 +741,10 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a0, cudaStream_t st)
                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
         }
         if (tma) {
-            switch (a.lg) {
-            case 12: ntt_inv_tma_kernel<12><<<grid, N >> 4, smp, st>>>(a, tmap); break;
-            case 13: ntt_inv_tma_kernel<13><<<grid, N >> 4, smp, st>>>(a, tmap); break;
-            default: ntt_inv_tma_kernel<14><<<grid, N >> 4, smp, st>>>(a, tmap); break;
-            }
+            if (a.lg == 12)
+                ntt_inv_tma_kernel<12><<<grid, N >> 4, smp, st>>>(a, tmap);
+            else
+                ntt_inv_tma_kernel<13><<<grid, N >> 4, smp, st>>>(a, tmap);
         } else {
             switch (a.lg) {
             case 12: ntt_inv_persist_kernel<12><<<grid, N >> 4, smp, st>>>(a); break;

@@ -59,9 +59,9 @@ def test_status_codes_and_recovery(ctx):
     with pytest.raises(PmlgError) as e:
         pml_gb300.nmod_poly_mat_pmbasis(F, 16, [0] * 4, P998 - 1, ctx=ctx)   # not a prime
     assert e.value.status == EBADMOD
-    F65 = to_dev(oracle.rand_poly_mat(65, 2, 16, P998, 5))
+    Fbig = to_dev(np.zeros((1025, 2, 16), dtype=np.uint64))
     with pytest.raises(PmlgError) as e:
-        pml_gb300.nmod_poly_mat_pmbasis(F65, 16, [0] * 65, P998, ctx=ctx)    # m > 64
+        pml_gb300.nmod_poly_mat_pmbasis(Fbig, 16, [0] * 1025, P998, ctx=ctx)    # m > 1024
     assert e.value.status == EUNSUP
     with pytest.raises(PmlgError) as e:
         pml_gb300.nmod_poly_mat_mulmid(A, A, -1, 4, P998, ctx=ctx)
@@ -81,17 +81,17 @@ def test_follow_on_status_codes(ctx):
     L = ctx.lib
     st = _stream()
     i64, nul, ic = C.c_int64(0), C.c_int64(0), C.c_int(0)
-    sh = (C.c_int64 * 65)()
-    piv = (C.c_int64 * 65)()
+    sh = (C.c_int64 * 1025)()
+    piv = (C.c_int64 * 1025)()
     P = torch.zeros((65, 2, 4), dtype=torch.int64, device="cuda")
     K = torch.zeros((65, 65, 8), dtype=torch.int64, device="cuda")
-    # kernel basis: m > 64, a composite modulus
-    assert L.pmlg_kernel_zls(ctx.handle, K.data_ptr(), 8, C.byref(i64), piv, sh, P.data_ptr(), 65, 2, 4, P998,
+    # kernel basis: m > 1024 (refused before any device access), a composite modulus
+    assert L.pmlg_kernel_zls(ctx.handle, K.data_ptr(), 8, C.byref(i64), piv, sh, P.data_ptr(), 1025, 2, 4, P998,
                              C.byref(nul), st) == EUNSUP
     assert L.pmlg_kernel_zls(ctx.handle, K.data_ptr(), 8, C.byref(i64), piv, sh, P.data_ptr(), 4, 2, 4, P998 - 1,
                              C.byref(nul), st) == EBADMOD
-    # truncated inverse and Dixon: n > 32; Dixon output shorter than ceil(sigma / order) * order
-    assert L.pmlg_inv_trunc(ctx.handle, K.data_ptr(), P.data_ptr(), 33, 1, 4, P998, C.byref(ic), st) == EUNSUP
+    # truncated inverse and Dixon: n > 512; Dixon output shorter than ceil(sigma / order) * order
+    assert L.pmlg_inv_trunc(ctx.handle, K.data_ptr(), P.data_ptr(), 513, 1, 4, P998, C.byref(ic), st) == EUNSUP
     assert L.pmlg_dixon(ctx.handle, K.data_ptr(), 7, P.data_ptr(), P.data_ptr(), 2, 1, 1, 1, 4, 8, P998,
                         C.byref(ic), st) == EINVAL
     # Popov basis: a capacity below order + 1; layout: an output shorter than the truncation
