@@ -869,7 +869,7 @@ def run_pml(args):
     # batched uneven products (every form, CUDA events around each call)
     extra = {} if args.no_extra else {
         "pointwise_batch": measure_pointwise_batch(ctx, dev, st, FORMS, rank),
-        "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS, rank),
+        "batched_uneven": measure_batched_uneven(ctx, dev, st, FORMS + (("auto", pml_gb300.FORM_AUTO),), rank),
         "kernel_basis": measure_kernel_basis(ctx, dev, st, rank),
         "layout_conversion": measure_layout(ctx, dev, st, rank, peaks.get("hbm_gbs")),
         "dot_products": measure_dot_products(ctx, dev, st, rank, peaks.get("hbm_gbs")),

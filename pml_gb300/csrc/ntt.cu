@@ -193,6 +193,20 @@ __device__ __forceinline__ void smem_to_regs_t(uint32_t (&v)[16], const uint32_t
     for (int s = 0; s < 16; s++) v[s] = p[grp_poff<G, LLS>(s)];
 }
 
+// Barriers between groups.  A group reads its layout from shared memory and writes
+// its results back in the same layout, so a thread only overwrites words it read
+// itself: the one hazard is the next group reading words other threads wrote (one
+// barrier per exchange).  From N = 512 on, a layout is warp-local when every warp
+// covers the same 512 consecutive residues ([512w, 512w + 512)) in it: the radix-16
+// layouts with sub-transforms spaced at most 32 apart, and the 16-consecutive layout
+// of a shorter group.  An exchange between two warp-local layouts needs only the
+// warp's own barrier.
+template <int LG, int G, int LLS>
+__device__ __forceinline__ constexpr bool warp_local_layout()
+{
+    return LG >= 9 && (G < 4 || LLS <= 5);
+}
+
 template <int LG, int GI, bool ZH>
 __device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
 {
@@ -200,34 +214,38 @@ __device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t
         using Gm = FwdGeom<LG, GI>;
         constexpr bool TW = Gm::G == 4 && Gm::LLS > 0;
         if constexpr (GI > 0) {
-            __syncthreads();
+            using Gp = FwdGeom<LG, GI - 1>;
+            if constexpr (warp_local_layout<LG, Gp::G, Gp::LLS>() && warp_local_layout<LG, Gm::G, Gm::LLS>())
+                __syncwarp();
+            else
+                __syncthreads();
             smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
         }
         dif_const<Gm::G, ZH && GI == 0, TW>(v, T);
         if constexpr (TW) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
-        if constexpr (GI < Gm::NG - 1) {
-            __syncthreads();   // everyone done reading the previous layout
-            regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
-        }
+        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
         fwd_groups<LG, GI + 1, ZH>(v, x, t, T);
     }
 }
 
+// The first group writes its layout without a barrier: a caller that reuses x for
+// another transform separates the last reads of the previous one from it.
 template <int LG, int GI>
 __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
 {
     if constexpr (GI < InvGeom<LG, 0>::NG) {
         using Gm = InvGeom<LG, GI>;
         if constexpr (GI > 0) {
-            __syncthreads();
+            using Gp = InvGeom<LG, GI - 1>;
+            if constexpr (warp_local_layout<LG, Gp::G, Gp::LLS>() && warp_local_layout<LG, Gm::G, Gm::LLS>())
+                __syncwarp();
+            else
+                __syncthreads();
             smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
         }
         if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
         dit_const<Gm::G>(v, T);
-        if constexpr (GI < Gm::NG - 1) {
-            __syncthreads();
-            regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
-        }
+        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
         inv_groups<LG, GI + 1>(v, x, t, T);
     }
 }
@@ -461,6 +479,7 @@ ntt_inv_persist_kernel(NttInvArgs a)
             v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
         }
         if (e + gridDim.x < a.nent) prefetch(e + gridDim.x);
+        __syncthreads();   // the previous transform's last reads of x are done
         inv_groups<LG, 0>(v, x, t, T);
         inv_store<LG>(v, a, e, j, t, T.q);
     }

@@ -349,7 +349,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
 {
     const uint32_t addr = (uint32_t)__cvta_generic_to_shared(b);
     uint64_t t0 = 0;
-    for (int it = 0; it < (1 << 26); it++) {
+    for (int it = 0; it < (1 << 30); it++) {
         uint32_t done;
         if (F16_SUSPEND_NS)
             asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}"
@@ -358,12 +358,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
             asm volatile("{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
                          : "=r"(done) : "r"(addr), "r"(parity) : "memory");
         if (done) return true;
-        if (abort && *abort) return false;
-        const uint64_t now = globaltimer_ns();
-        if (it == 0)
-            t0 = now;
-        else if (now - t0 > F16_WAIT_NS)
-            break;
+        if ((it & 63) == 0) {
+            if (abort && *abort) return false;
+            const uint64_t now = globaltimer_ns();
+            if (it == 0)
+                t0 = now;
+            else if (now - t0 > F16_WAIT_NS)
+                break;
+        }
     }
     if (abort) *abort = 1;
     return false;
