@@ -331,6 +331,9 @@ static int check_common(pmlg_ctx *ctx, const void *C, const void *A, const void 
 #ifndef PMLG_HOST_ROW_BLOCKS
 #define PMLG_HOST_ROW_BLOCKS 4
 #endif
+#ifndef PMLG_HOST_2D
+#define PMLG_HOST_2D 1      // host-buffer products with one NTT prime: 2 x 2 blocks of C
+#endif
 // row blocks of the host-buffer product's pipeline (events used: 2 + 4 + 2 * blocks)
 constexpr int kHostRowBlocks = PMLG_HOST_ROW_BLOCKS;
 static_assert(2 + 4 + 2 * kHostRowBlocks <= pmlg_ctx::kHostEvents, "host pipeline events");
@@ -442,6 +445,108 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
         return cudaEventRecord(*out, s) == cudaSuccess ? PMLG_OK : PMLG_ECUDA;
     };
     cudaEvent_t e;
+    if (PMLG_HOST_2D && plan.direct && r >= 2 && c >= 2) {
+        // 2 x 2 blocks of C.  Block (I, J) needs only rows I of A and columns J of B, so
+        // the first block goes back to the host while the rest of the operands are still
+        // coming in: B columns 0, A rows 0 -> C00; B columns 1 -> C01; A rows 1 -> C10,
+        // C11.  Every block is an ordinary product of its own contiguous device copies
+        // (B's column blocks and C's blocks move as 2-D copies, one run of entries per
+        // row of entries), and each half of A and of B is transformed once.
+        const int64_t R0[3] = {0, r / 2, r}, C0[3] = {0, c / 2, c};
+        const int64_t N = 1ll << j.lg;
+        uint64_t *dBJ[2] = {dB, dB + k * C0[1] * len2};
+        uint64_t *dCB[2][2];
+        {
+            uint64_t *w = dC;
+            for (int ib = 0; ib < 2; ib++)
+                for (int jb = 0; jb < 2; jb++) {
+                    dCB[ib][jb] = w;
+                    w += (R0[ib + 1] - R0[ib]) * (C0[jb + 1] - C0[jb]) * clen;
+                }
+        }
+        // evaluations: A rows I, B columns J, C blocks (I, J), each in its own point-tiled layout
+        uint32_t *EA[2], *EB[2], *EC[2][2];
+        PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan) + 16 * 256));
+        {
+            char *w = (char *)ctx->ws.ptr;
+            auto take = [&](int64_t nent) {
+                uint32_t *r_ = (uint32_t *)w;
+                w += align256((size_t)(N * nent) * 4);
+                return r_;
+            };
+            for (int ib = 0; ib < 2; ib++) EA[ib] = take((R0[ib + 1] - R0[ib]) * k);
+            for (int jb = 0; jb < 2; jb++) EB[jb] = take(k * (C0[jb + 1] - C0[jb]));
+            for (int ib = 0; ib < 2; ib++)
+                for (int jb = 0; jb < 2; jb++) EC[ib][jb] = take((R0[ib + 1] - R0[ib]) * (C0[jb + 1] - C0[jb]));
+        }
+        // the product of block (I, J) and its buffers
+        auto block_job = [&](int ib, int jb, ProductJob &bj, ProductBufs &bb) {
+            bj = j;
+            bj.r = R0[ib + 1] - R0[ib];
+            bj.c = C0[jb + 1] - C0[jb];
+            bj.A = dA + R0[ib] * k * len1;
+            bj.B = dBJ[jb];
+            bj.C = dCB[ib][jb];
+            bb = b;
+            bb.EA = EA[ib];
+            bb.EB = EB[jb];
+            bb.EC = EC[ib][jb];
+            bb.R32 = nullptr;
+        };
+        PMLG_TRY(next_event(st, &e));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(hs, e, 0));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, e, 0));
+        cudaEvent_t bev[2], aev[2];
+        for (int q = 0; q < 4; q++) {   // B columns 0, A rows 0, B columns 1, A rows 1
+            const int h = q >> 1;
+            if ((q & 1) == 0) {
+                const int64_t bw = C0[h + 1] - C0[h];
+                PMLG_CUDA_TRY(cudaMemcpy2DAsync(dBJ[h], (size_t)(bw * len2) * 8, B + C0[h] * len2,
+                                                (size_t)(c * len2) * 8, (size_t)(bw * len2) * 8, (size_t)k,
+                                                cudaMemcpyHostToDevice, hs));
+                PMLG_TRY(next_event(hs, &bev[h]));
+            } else {
+                PMLG_TRY(h2d(ctx, dA + R0[h] * k * len1, A + R0[h] * k * len1,
+                             (size_t)((R0[h + 1] - R0[h]) * k * len1) * 8, hs));
+                PMLG_TRY(next_event(hs, &aev[h]));
+            }
+        }
+        auto run_block = [&](int ib, int jb) -> int {
+            ProductJob bj;
+            ProductBufs bb;
+            block_job(ib, jb, bj, bb);
+            PMLG_TRY(product_pointwise(ctx, bj, plan, bb, 0, bj.r, ctx->form, st));
+            PMLG_TRY(product_inverse(ctx, bj, plan, bb, 0, bj.r * bj.c, st));
+            cudaEvent_t ce;
+            PMLG_TRY(next_event(st, &ce));
+            PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, ce, 0));
+            PMLG_CUDA_TRY(cudaMemcpy2DAsync(C + (R0[ib] * c + C0[jb]) * clen, (size_t)(c * clen) * 8, bj.C,
+                                            (size_t)(bj.c * clen) * 8, (size_t)(bj.c * clen) * 8, (size_t)bj.r,
+                                            cudaMemcpyDeviceToHost, ds));
+            return PMLG_OK;
+        };
+        auto fwd_half = [&](int which, int h) -> int {   // A rows h (which 0) or B columns h (which 1)
+            ProductJob bj;
+            ProductBufs bb;
+            block_job(which == 0 ? h : 0, which == 0 ? 0 : h, bj, bb);
+            return product_forward(ctx, bj, plan, bb, which, 0, which == 0 ? bj.r * k : k * bj.c, st);
+        };
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, bev[0], 0));
+        PMLG_TRY(fwd_half(1, 0));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, aev[0], 0));
+        PMLG_TRY(fwd_half(0, 0));
+        PMLG_TRY(run_block(0, 0));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, bev[1], 0));
+        PMLG_TRY(fwd_half(1, 1));
+        PMLG_TRY(run_block(0, 1));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, aev[1], 0));
+        PMLG_TRY(fwd_half(0, 1));
+        PMLG_TRY(run_block(1, 0));
+        PMLG_TRY(run_block(1, 1));
+        PMLG_TRY(next_event(ds, &e));
+        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
+        return device_status(ctx, st);
+    }
     PMLG_TRY(next_event(st, &e));
     PMLG_CUDA_TRY(cudaStreamWaitEvent(hs, e, 0));
     PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, e, 0));
