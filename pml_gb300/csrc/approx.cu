@@ -899,7 +899,10 @@ static int leaf64_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F,
     a.AB = (uint64_t *)S.ar.alloc((size_t)(o + 1) * m * m * 8);
     a.E = e_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)n * m * 8);
     a.X = x_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)m * mn * 8);
-    if (!a.R || !a.AB || (!e_sh && !a.E) || (!x_sh && !a.X)) return PMLG_ENOMEM;
+    a.Xg = a.X;
+    a.sh = (long long *)S.ar.alloc((size_t)m * 8);
+    a.st = (int *)S.ar.alloc((size_t)(16 + 2 * m) * 4);
+    if (!a.R || !a.AB || (!e_sh && !a.E) || (!x_sh && !a.X) || !a.sh || !a.st) return PMLG_ENOMEM;
     a.F = F; a.ldF = ldF; a.flen = flen;
     a.out = out; a.ldo = ldo;
     a.shift = S.d_shift;

@@ -292,16 +292,299 @@ mbasis_leaf64_kernel(Leaf64Args a)
     if (tid == 0) *a.len_out = (unsigned long long)alen;
 }
 
+// ---------------------------------------------------------------------------
+// Stepped leaf: the same steps, as four launches per order step instead of one CTA
+// for the whole leaf.  The elimination (one CTA: the sequential chain of pivots) is
+// followed by the row updates of appbas and R, spread over the whole GPU, then by
+// the pivot rows times x; their state (shifts, pivot and non-pivot rows, X, rank,
+// the length of appbas) lives in global memory between the launches.  A step that
+// finds the nullity 0 finishes the leaf: every later launch returns at once.
+// ---------------------------------------------------------------------------
+
+// st[]: rank, nullity, alen, grow, finished, mode (0: nothing to do this step,
+// 1: update, 2: appbas times x^k and done), k; pivot rows at st + 16, non-pivot
+// rows at st + 16 + m
+enum { ST_RANK = 0, ST_NUL, ST_ALEN, ST_GROW, ST_FIN, ST_MODE, ST_K, ST_HDR = 16 };
+
+__global__ void l64s_init(Leaf64Args a)
+{
+    const int m = a.m, n = a.n, order = a.order;
+    const int64_t fl = a.flen < order ? a.flen : order;
+    const int64_t mm = (int64_t)m * m, mnn = (int64_t)m * n;
+    const int64_t tot_r = (int64_t)order * mnn, tot_a = (int64_t)(order + 1) * mm;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < tot_r + tot_a + m;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        if (idx < tot_r) {
+            const int64_t d = idx / mnn, rem = idx - d * mnn;
+            a.R[idx] = d < fl ? a.F[rem * a.ldF + d] : 0ull;
+        } else if (idx < tot_r + tot_a) {
+            const int64_t i = idx - tot_r;
+            a.AB[i] = (i < mm && (i / m) == (i % m)) ? 1ull : 0ull;
+        } else {
+            a.sh[idx - tot_r - tot_a] = a.shift[idx - tot_r - tot_a];
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < ST_HDR) a.st[threadIdx.x] = threadIdx.x == ST_ALEN ? 1 : 0;
+}
+
+// shared memory of the elimination CTA: shifts, factors, inverses, E (when it fits),
+// then the integer arrays (as l64_smem with X in global memory)
+__global__ void __launch_bounds__(L64_THREADS)
+l64s_elim(Leaf64Args a, int ord)
+{
+    extern __shared__ __align__(16) unsigned char l64s[];
+    __shared__ int s_pl, s_rank, s_nn, s_stop;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int m = a.m, n = a.n, order = a.order;
+    const int mn = m < n ? m : n;
+    const M64 M{a.p, a.pneg, a.r2, a.two};
+    int *st = a.st;
+    if (tid == 0) {
+        s_stop = st[ST_FIN];
+        if (s_stop) {
+            st[ST_MODE] = 0;
+        } else {
+            st[ST_ALEN] += st[ST_GROW];   // the previous step's growth
+            st[ST_GROW] = 0;
+        }
+    }
+    __syncthreads();
+    if (s_stop) return;
+    unsigned char *sp = l64s;
+    auto take = [&](size_t bytes) {
+        unsigned char *r = sp;
+        sp += l64_al(bytes);
+        return r;
+    };
+    long long *sh = (long long *)take((size_t)m * 8);
+    uint64_t *fac = (uint64_t *)take((size_t)n * 8);
+    uint64_t *inv = (uint64_t *)take((size_t)mn * 8);
+    uint64_t *E = a.E ? a.E : (uint64_t *)take((size_t)n * m * 8);
+    int *perm = (int *)take((size_t)m * 4);
+    int *pivlane = (int *)take((size_t)m * 4);
+    int *pivcol = (int *)take((size_t)m * 4);
+    int *nonpiv = (int *)take((size_t)m * 4);
+    (void)take((size_t)m * 4);
+    (void)take((size_t)m * 4);
+    int *used = (int *)take((size_t)n * 4);
+    int *pivrow = st + ST_HDR, *nprow = st + ST_HDR + m;
+    const int64_t mnn = (int64_t)m * n;
+
+    for (int t = tid; t < m; t += nth) sh[t] = a.sh[t];
+    if (tid == 0) { s_rank = 0; s_nn = 0; }
+    for (int j = tid; j < n; j += nth) used[j] = 0;
+    __syncthreads();
+    // 1. stable sort of (shift, index): rank by counting
+    for (int t = tid; t < m; t += nth) {
+        const long long v = sh[t];
+        int r = 0;
+        for (int i = 0; i < m; i++) r += (sh[i] < v) || (sh[i] == v && i < t);
+        perm[r] = t;
+    }
+    __syncthreads();
+    for (int64_t idx = tid; idx < mnn; idx += nth) {
+        const int r = (int)(idx / n), j = (int)(idx - (int64_t)r * n);
+        E[(int64_t)j * m + r] = a.R[((int64_t)ord * m + perm[r]) * n + j];
+    }
+    __syncthreads();
+    // 2. division-free Gauss-Jordan on E (n rows, m columns)
+    for (int c = 0; c < m; c++) {
+        if (tid < 32) {
+            int pl = -1;
+            for (int base = 0; base < n && pl < 0; base += 32) {
+                const int l = base + tid;
+                const uint64_t v = (l < n && !used[l]) ? E[(int64_t)l * m + c] : 0ull;
+                const unsigned b = __ballot_sync(0xffffffffu, v != 0);
+                if (b) pl = base + __ffs(b) - 1;
+            }
+            if (tid == 0) {
+                s_pl = pl;
+                if (pl < 0) {
+                    nonpiv[s_nn++] = c;
+                } else {
+                    used[pl] = 1;
+                    pivlane[s_rank] = pl;
+                    pivcol[s_rank] = c;
+                    s_rank++;
+                }
+            }
+        }
+        for (int j = tid; j < n; j += nth) fac[j] = E[(int64_t)j * m + c];
+        __syncthreads();
+        const int pl = s_pl, rk = s_rank;
+        if (pl >= 0) {
+            const uint64_t pv = E[(int64_t)pl * m + c];
+            for (int64_t idx = tid; idx < mnn; idx += nth) {
+                const int j = (int)(idx / m), cc = (int)(idx - (int64_t)j * m);
+                if (j == pl) continue;
+                E[idx] = M.sub(M.mul(pv, E[idx]), M.mul(fac[j], E[(int64_t)pl * m + cc]));
+            }
+        }
+        __syncthreads();
+        if (rk == n) {
+            const int nn0 = s_nn;
+            for (int t = tid; t < m - 1 - c; t += nth) nonpiv[nn0 + t] = c + 1 + t;
+            __syncthreads();
+            if (tid == 0) s_nn = nn0 + (m - 1 - c);
+            __syncthreads();
+            break;
+        }
+    }
+    const int rank = s_rank, nullity = m - rank;
+    if (nullity == 0) {
+        // appbas = x^(order-ord) * appbas (in the update launch), shift += order - ord; done
+        const int k = order - ord;
+        for (int t = tid; t < m; t += nth) a.sh[t] = sh[t] + k;
+        if (tid == 0) { st[ST_FIN] = 1; st[ST_MODE] = 2; st[ST_K] = k; }
+        return;
+    }
+    if (rank == 0) {
+        if (tid == 0) st[ST_MODE] = 0;   // zero residual: nothing changes
+        return;
+    }
+    for (int b = tid; b < rank; b += nth) {
+        inv[b] = M.inv(E[(int64_t)pivlane[b] * m + pivcol[b]]);
+        pivrow[b] = perm[pivcol[b]];
+    }
+    for (int ia = tid; ia < nullity; ia += nth) nprow[ia] = perm[nonpiv[ia]];
+    __syncthreads();
+    for (int64_t idx = tid; idx < (int64_t)nullity * rank; idx += nth) {
+        const int ia = (int)(idx / rank), b = (int)(idx - (int64_t)ia * rank);
+        const uint64_t x = M.mulmod(E[(int64_t)pivlane[b] * m + nonpiv[ia]], inv[b]);
+        a.Xg[idx] = M.tomont(M.neg(x));
+    }
+    for (int t = tid; t < m; t += nth) {
+        // the shifts of the pivot rows + 1 (pivrow is in global memory: read this CTA's copy)
+        long long v = sh[t];
+        for (int b = 0; b < rank; b++) v += pivrow[b] == t ? 1 : 0;
+        a.sh[t] = v;
+    }
+    if (tid == 0) { st[ST_RANK] = rank; st[ST_NUL] = nullity; st[ST_MODE] = 1; }
+}
+
+// non-pivot rows += X * pivot rows (appbas d < alen, R ord < d < order); the growth test
+// on the pivot rows' top coefficient; or, finishing, appbas times x^k
+__global__ void l64s_update(Leaf64Args a, int ord)
+{
+    const int *st = a.st;
+    const int mode = st[ST_MODE];
+    if (mode == 0) return;
+    const int m = a.m, n = a.n, order = a.order;
+    const int64_t mm = (int64_t)m * m, mnn = (int64_t)m * n;
+    const int alen = st[ST_ALEN];
+    const int64_t g0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, gs = (int64_t)gridDim.x * blockDim.x;
+    if (mode == 2) {
+        const int k = st[ST_K];
+        for (int64_t idx = g0; idx < mm; idx += gs) {
+            for (int d = alen - 1; d >= 0; d--) a.AB[(int64_t)(d + k) * mm + idx] = a.AB[(int64_t)d * mm + idx];
+            for (int d = 0; d < k; d++) a.AB[(int64_t)d * mm + idx] = 0;
+        }
+        return;
+    }
+    const M64 M{a.p, a.pneg, a.r2, a.two};
+    const int rank = st[ST_RANK], nullity = st[ST_NUL];
+    const int *pivrow = st + ST_HDR, *nprow = st + ST_HDR + m;
+    const int64_t nab = (int64_t)nullity * alen * m;
+    const int64_t nR = (int64_t)nullity * (order - ord - 1) * n;
+    for (int64_t idx = g0; idx < nab + nR; idx += gs) {
+        uint64_t *base;
+        int col, width, ia;
+        if (idx < nab) {
+            ia = (int)(idx / ((int64_t)alen * m));
+            const int64_t rem = idx - (int64_t)ia * alen * m;
+            const int64_t coef = rem / m;
+            col = (int)(rem - coef * m);
+            width = m;
+            base = a.AB + coef * mm;
+        } else {
+            const int64_t j2 = idx - nab;
+            ia = (int)(j2 / ((int64_t)(order - ord - 1) * n));
+            const int64_t rem = j2 - (int64_t)ia * (order - ord - 1) * n;
+            const int64_t coef = ord + 1 + rem / n;
+            col = (int)(rem % n);
+            width = n;
+            base = a.R + coef * mnn;
+        }
+        const int row = nprow[ia];
+        const uint64_t *xr = a.Xg + (int64_t)ia * rank;
+        uint64_t acc = base[(int64_t)row * width + col];
+        for (int b = 0; b < rank; b++) acc = M.add(acc, M.mul(xr[b], base[(int64_t)pivrow[b] * width + col]));
+        base[(int64_t)row * width + col] = acc;
+    }
+    // the pivot rows are not written above: their top coefficient decides the growth
+    int grow = 0;
+    for (int64_t idx = g0; idx < (int64_t)rank * m; idx += gs) {
+        const int b = (int)(idx / m), col = (int)(idx - (int64_t)b * m);
+        if (a.AB[(int64_t)(alen - 1) * mm + (int64_t)pivrow[b] * m + col] != 0) grow = 1;
+    }
+    if (__syncthreads_or(grow) && threadIdx.x == 0) atomicOr(a.st + ST_GROW, 1);
+}
+
+// pivot rows times x in appbas and in R; or, finishing, the length of appbas + k
+__global__ void l64s_shift(Leaf64Args a, int ord)
+{
+    int *st = a.st;
+    const int mode = st[ST_MODE];
+    if (mode == 2) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) st[ST_ALEN] += st[ST_K];
+        return;
+    }
+    if (mode != 1) return;
+    const int m = a.m, n = a.n, order = a.order;
+    const int64_t mm = (int64_t)m * m, mnn = (int64_t)m * n;
+    const int rank = st[ST_RANK], nlen = st[ST_ALEN] + st[ST_GROW];
+    const int *pivrow = st + ST_HDR;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < (int64_t)rank * (m + n);
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int b = (int)(idx / (m + n)), col = (int)(idx - (int64_t)b * (m + n));
+        const int row = pivrow[b];
+        if (col < m) {
+            for (int d = nlen - 1; d > 0; d--)
+                a.AB[(int64_t)d * mm + (int64_t)row * m + col] = a.AB[(int64_t)(d - 1) * mm + (int64_t)row * m + col];
+            a.AB[(int64_t)row * m + col] = 0;
+        } else {
+            const int j = col - m;
+            for (int d = order - 1; d > ord; d--)
+                a.R[(int64_t)d * mnn + (int64_t)row * n + j] = a.R[(int64_t)(d - 1) * mnn + (int64_t)row * n + j];
+        }
+    }
+}
+
+// appbas out (entry-major, zero past its length), the shifts and the length
+__global__ void l64s_final(Leaf64Args a)
+{
+    const int m = a.m;
+    const int64_t mm = (int64_t)m * m;
+    const int alen = a.st[ST_ALEN] + a.st[ST_GROW];
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < mm * a.ldo;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = idx / a.ldo, d = idx - e * a.ldo;
+        a.out[idx] = d < alen ? a.AB[d * mm + e] : 0ull;
+    }
+    if (blockIdx.x == 0) {
+        for (int t = threadIdx.x; t < m; t += blockDim.x) a.shift[t] = a.sh[t];
+        if (threadIdx.x == 0) *a.len_out = (unsigned long long)alen;
+    }
+}
+
+// the stepped leaf pays four launches per order step; it takes over from the one-CTA
+// kernel when the rows are many enough that the updates outweigh the launches
+static bool l64_stepped(int m, int n)
+{
+    return m >= 24 || (int64_t)m * (m + n) >= 1536;
+}
+
 size_t leaf64_scratch_bytes(int m, int n, int order, bool *e_shared, bool *x_shared)
 {
     const size_t mn = m < n ? m : n;
     const bool e_sh = l64_smem(m, n, true, false) <= L64_SMEM_BUDGET;
-    const bool x_sh = l64_smem(m, n, e_sh, true) <= L64_SMEM_BUDGET;
+    const bool x_sh = !l64_stepped(m, n) && l64_smem(m, n, e_sh, true) <= L64_SMEM_BUDGET;
     if (e_shared) *e_shared = e_sh;
     if (x_shared) *x_shared = x_sh;
     size_t b = l64_al((size_t)order * m * n * 8) + l64_al((size_t)(order + 1) * m * m * 8);
     if (!e_sh) b += l64_al((size_t)n * m * 8);
     if (!x_sh) b += l64_al((size_t)m * mn * 8);
+    b += l64_al((size_t)m * 8) + l64_al((size_t)(ST_HDR + 2 * m) * 4);   // shifts, step state
     return b;
 }
 
@@ -324,6 +607,39 @@ void leaf64_set_modulus(Leaf64Args &a, uint64_t p)
 
 int leaf64_launch(pmlg_ctx *ctx, const Leaf64Args &a, cudaStream_t st)
 {
+    if (l64_stepped(a.m, a.n)) {
+        const int m = a.m, n = a.n, order = a.order;
+        const size_t smem = l64_smem(m, n, a.E == nullptr, false);
+        PMLG_CUDA_TRY(cudaFuncSetAttribute(l64s_elim, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        auto grid_for = [&](int64_t work) {
+            int64_t g = (work + 255) / 256;
+            const int64_t cap = (int64_t)ctx->sm_count * 8;
+            return (unsigned)(g < 1 ? 1 : (g > cap ? cap : g));
+        };
+        const int64_t mm = (int64_t)m * m, mnn = (int64_t)m * n;
+        prof_begin(ctx, "mbasis_leaf64_init", st);
+        l64s_init<<<grid_for((int64_t)order * mnn + (int64_t)(order + 1) * mm + m), 256, 0, st>>>(a);
+        prof_end(ctx, st);
+        const unsigned gu = grid_for((int64_t)m * (m * (int64_t)(order + 1) + n * (int64_t)order));
+        const unsigned gsh = grid_for((int64_t)m * (m + n));
+        for (int ord = 0; ord < order; ord++) {
+            prof_begin(ctx, "mbasis_leaf64_elim", st);
+            l64s_elim<<<1, L64_THREADS, smem, st>>>(a, ord);
+            prof_end(ctx, st);
+            prof_begin(ctx, "mbasis_leaf64_update", st);
+            l64s_update<<<gu, 256, 0, st>>>(a, ord);
+            prof_end(ctx, st);
+            prof_begin(ctx, "mbasis_leaf64_shift", st);
+            l64s_shift<<<gsh, 256, 0, st>>>(a, ord);
+            prof_end(ctx, st);
+        }
+        prof_begin(ctx, "mbasis_leaf64_final", st);
+        l64s_final<<<grid_for(mm * a.ldo), 256, 0, st>>>(a);
+        prof_end(ctx, st);
+        count_launch(ctx, (unsigned)(3 * order + 2));
+        PMLG_CUDA_TRY(cudaGetLastError());
+        return PMLG_OK;
+    }
     const size_t smem = l64_smem(a.m, a.n, a.E == nullptr, a.X == nullptr);
     PMLG_CUDA_TRY(cudaFuncSetAttribute(mbasis_leaf64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     prof_begin(ctx, "mbasis_leaf64", st);

@@ -21,6 +21,10 @@ struct Leaf64Args
     uint64_t *X;            // [m][min(m, n)] scratch in global memory, or null: in shared memory
     int64_t *shift;         // device, m entries: in and out
     unsigned long long *len_out;   // device: appbas' length
+    // the stepped leaf (one launch per phase of every step) keeps its state in global memory
+    uint64_t *Xg;           // [m][min(m, n)]: X of the current step, Montgomery form
+    long long *sh;          // [m]: the shifts
+    int *st;                // [16 + 2m]: step state, then the pivot rows and the non-pivot rows
     int m, n, order;
     uint64_t p;
     uint64_t pneg;          // -p^-1 mod 2^64 (p odd)
