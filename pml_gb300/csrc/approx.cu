@@ -864,7 +864,7 @@ static bool wide_leaf(int64_t m, int64_t n, uint64_t p)
 static size_t pm_arena_bytes(int64_t m, int64_t n, int64_t o, int64_t leaf, bool wide)
 {
     if (o <= leaf) {
-        if (wide) return leaf64_scratch_bytes((int)m, (int)n, (int)o, nullptr, nullptr) + 1024;
+        if (wide) return leaf64_scratch_bytes((int)m, (int)n, (int)o) + 1024;
         return (size_t)(o * m * n + (o + 1) * m * m) * 4 + 1024;
     }
     const int64_t o1 = o >> 1, o2 = o - o1;
@@ -891,18 +891,16 @@ static int leaf64_run(PmState &S, uint64_t *out, int64_t ldo, const uint64_t *F,
 {
     const size_t mark = S.ar.top;
     const int m = (int)S.m, n = (int)S.n, o = (int)order;
-    const int mn = m < n ? m : n;
-    bool e_sh = false, x_sh = false;
-    leaf64_scratch_bytes(m, n, o, &e_sh, &x_sh);
+    const Leaf64Sizes z = leaf64_sizes(m, n, o);
     Leaf64Args a{};
-    a.R = (uint64_t *)S.ar.alloc((size_t)o * m * n * 8 + 8);
-    a.AB = (uint64_t *)S.ar.alloc((size_t)(o + 1) * m * m * 8);
-    a.E = e_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)n * m * 8);
-    a.X = x_sh ? nullptr : (uint64_t *)S.ar.alloc((size_t)m * mn * 8);
+    a.R = (uint64_t *)S.ar.alloc(z.R);
+    a.AB = (uint64_t *)S.ar.alloc(z.AB);
+    a.E = z.E ? (uint64_t *)S.ar.alloc(z.E) : nullptr;
+    a.X = z.X ? (uint64_t *)S.ar.alloc(z.X) : nullptr;
     a.Xg = a.X;
-    a.sh = (long long *)S.ar.alloc((size_t)m * 8);
-    a.st = (int *)S.ar.alloc((size_t)(16 + 2 * m) * 4);
-    if (!a.R || !a.AB || (!e_sh && !a.E) || (!x_sh && !a.X) || !a.sh || !a.st) return PMLG_ENOMEM;
+    a.sh = (long long *)S.ar.alloc(z.sh);
+    a.st = (int *)S.ar.alloc(z.st);
+    if (!a.R || !a.AB || (z.E && !a.E) || (z.X && !a.X) || !a.sh || !a.st) return PMLG_ENOMEM;
     a.F = F; a.ldF = ldF; a.flen = flen;
     a.out = out; a.ldo = ldo;
     a.shift = S.d_shift;
