@@ -557,8 +557,15 @@ ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
 
 // ---------------------------------------------------------------------------
 
-__global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int64_t nent, int64_t cnt,
-                           uint64_t *__restrict__ out64, int64_t out_ld, int64_t out_cap)
+// Garner's CRT of T residues, one instantiation per prime count so the residues and
+// the mixed-radix digits stay in registers; every residue of a coefficient is loaded
+// before any arithmetic.  The primes are in (2^29.8, 2^30): a Shoup product is below
+// 2 q_j and the running value below 2 q_j + 2^30 < 2^32, so the inner Horner steps
+// need no reduction, and two conditional subtractions bring it below q_j.
+template <int T>
+__global__ void __launch_bounds__(256)
+crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int64_t nent, int64_t cnt,
+           uint64_t *__restrict__ out64, int64_t out_ld, int64_t out_cap)
 {
     // entries along grid y, coefficients along x (no 64-bit division per element)
     for (int64_t e = blockIdx.y; e < nent; e += gridDim.y)
@@ -568,22 +575,22 @@ __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int
             out64[e * out_ld + d] = 0;
             continue;
         }
-        uint32_t c[kMaxPrimes];
-        c[0] = res32[e * cnt + d];
-        for (int j = 1; j < plan.t; j++) {
+        uint32_t c[T];
+#pragma unroll
+        for (int j = 0; j < T; j++) c[j] = __ldg(res32 + (j * nent + e) * cnt + d);
+#pragma unroll
+        for (int j = 1; j < T; j++) {
             const uint32_t qj = plan.q[j];
-            // value of c_0 + c_1 q_0 + ... + c_{j-1} q_0..q_{j-2} modulo q_j
+            // c_0 + c_1 q_0 + ... + c_{j-1} q_0..q_{j-2} modulo q_j
             uint32_t v = c[j - 1];
-            for (int l = j - 2; l >= 0; l--) {
-                v = v >= qj ? v - qj : v;
-                v = shoup_mul(v, plan.qmod[j][l], plan.qmodq[j][l], qj) + c[l];   // < 2 qj + 2^30
-                while (v >= qj) v -= qj;
-            }
-            while (v >= qj) v -= qj;
-            const uint32_t r = res32[(j * nent + e) * cnt + d];
-            uint32_t diff = r >= v ? r - v : r + qj - v;
-            uint32_t cj = shoup_mul(diff, plan.ginv[j], plan.ginvq[j], qj);
-            c[j] = cj >= qj ? cj - qj : cj;
+#pragma unroll
+            for (int l = j - 2; l >= 0; l--) v = shoup_mul(v, plan.qmod[j][l], plan.qmodq[j][l], qj) + c[l];
+            v = min(v, v - 2 * qj);
+            v = min(v, v - qj);
+            const uint32_t r = c[j];
+            const uint32_t diff = r + qj - v;   // in [1, 2 q_j)
+            const uint32_t cj = shoup_mul(diff, plan.ginv[j], plan.ginvq[j], qj);
+            c[j] = min(cj, cj - qj);
         }
         const uint64_t p = plan.p;
         uint64_t res;
@@ -593,8 +600,9 @@ __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int
                 uint64_t r = v - __umul64hi(v, plan.onepq) * p;
                 return r >= p ? r - p : r;
             };
-            uint64_t x = red(c[plan.t - 1]);
-            for (int l = plan.t - 2; l >= 0; l--) {
+            uint64_t x = red(c[T - 1]);
+#pragma unroll
+            for (int l = T - 2; l >= 0; l--) {
                 x = x * plan.qp[l] - __umul64hi(x, plan.qpq[l]) * p;
                 x = x >= p ? x - p : x;
                 const uint64_t cl = red(c[l]);
@@ -603,8 +611,9 @@ __global__ void crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int
             }
             res = x;
         } else {
-            unsigned __int128 x = c[plan.t - 1] % p;
-            for (int l = plan.t - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
+            unsigned __int128 x = c[T - 1] % p;
+#pragma unroll
+            for (int l = T - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
             res = (uint64_t)x;
         }
         out64[e * out_ld + d] = res;
@@ -788,8 +797,16 @@ int crt_combine(pmlg_ctx *ctx, const CrtPlan &plan, const uint32_t *res32, int64
     int64_t bx = (out_cap + 255) / 256;
     const int64_t cap = ((int64_t)ctx->sm_count * 16 + by - 1) / by;   // about 16 CTAs per SM in all
     if (bx > cap) bx = cap;
+    const dim3 grid((unsigned)bx, (unsigned)by);
     prof_begin(ctx, "crt", st);
-    crt_kernel<<<dim3((unsigned)bx, (unsigned)by), 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap);
+    switch (plan.t) {
+    case 1: crt_kernel<1><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    case 2: crt_kernel<2><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    case 3: crt_kernel<3><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    case 4: crt_kernel<4><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    case 5: crt_kernel<5><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    default: crt_kernel<6><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    }
     prof_end(ctx, st);
     count_launch(ctx);
     PMLG_CUDA_TRY(cudaGetLastError());
