@@ -332,11 +332,20 @@ static int check_common(pmlg_ctx *ctx, const void *C, const void *A, const void 
 #define PMLG_HOST_ROW_BLOCKS 4
 #endif
 #ifndef PMLG_HOST_2D
-#define PMLG_HOST_2D 1      // host-buffer products with one NTT prime: 2 x 2 blocks of C
+#define PMLG_HOST_2D 1      // host-buffer products with one NTT prime: blocks of C in both directions
+#endif
+#ifndef PMLG_HOST_BR
+#define PMLG_HOST_BR 2      // row blocks of C (and A) in that pipeline
+#endif
+#ifndef PMLG_HOST_BC
+#define PMLG_HOST_BC 3      // column blocks of C (and B)
 #endif
 // row blocks of the host-buffer product's pipeline (events used: 2 + 4 + 2 * blocks)
 constexpr int kHostRowBlocks = PMLG_HOST_ROW_BLOCKS;
 static_assert(2 + 4 + 2 * kHostRowBlocks <= pmlg_ctx::kHostEvents, "host pipeline events");
+constexpr int kHostBR = PMLG_HOST_BR, kHostBC = PMLG_HOST_BC;
+static_assert(kHostBR >= 1 && kHostBC >= 1 && 2 + kHostBR + kHostBC + kHostBR * kHostBC <= pmlg_ctx::kHostEvents,
+              "host pipeline events");
 
 static int h2d(pmlg_ctx *ctx, void *dst, const void *src, size_t bytes, cudaStream_t st)
 {
@@ -445,28 +454,33 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
         return cudaEventRecord(*out, s) == cudaSuccess ? PMLG_OK : PMLG_ECUDA;
     };
     cudaEvent_t e;
-    if (PMLG_HOST_2D && plan.direct && r >= 2 && c >= 2) {
-        // 2 x 2 blocks of C.  Block (I, J) needs only rows I of A and columns J of B, so
-        // the first block goes back to the host while the rest of the operands are still
-        // coming in: B columns 0, A rows 0 -> C00; B columns 1 -> C01; A rows 1 -> C10,
-        // C11.  Every block is an ordinary product of its own contiguous device copies
-        // (B's column blocks and C's blocks move as 2-D copies, one run of entries per
-        // row of entries), and each half of A and of B is transformed once.
-        const int64_t R0[3] = {0, r / 2, r}, C0[3] = {0, c / 2, c};
+    if (PMLG_HOST_2D && plan.direct && r >= kHostBR && c >= kHostBC && kHostBR * kHostBC > 1) {
+        // BR x BC blocks of C.  Block (I, J) needs only rows I of A and columns J of B,
+        // so the first block goes back to the host while the rest of the operands are
+        // still coming in.  The copies go B columns 0, A rows 0, B columns 1, A rows 1,
+        // ...; after B columns s come the blocks (I < s, s), after A rows s the blocks
+        // (s, J <= s).  Every block is an ordinary product of its own contiguous device
+        // copies (B's column blocks and C's blocks move as 2-D copies, one run of entries
+        // per row of entries), and each block of A and of B is transformed once.
+        constexpr int BR = kHostBR, BC = kHostBC;
+        int64_t R0[BR + 1], C0[BC + 1];
+        for (int ib = 0; ib <= BR; ib++) R0[ib] = r * ib / BR;
+        for (int jb = 0; jb <= BC; jb++) C0[jb] = c * jb / BC;
         const int64_t N = 1ll << j.lg;
-        uint64_t *dBJ[2] = {dB, dB + k * C0[1] * len2};
-        uint64_t *dCB[2][2];
+        uint64_t *dBJ[BC];
+        for (int jb = 0; jb < BC; jb++) dBJ[jb] = dB + k * C0[jb] * len2;
+        uint64_t *dCB[BR][BC];
         {
             uint64_t *w = dC;
-            for (int ib = 0; ib < 2; ib++)
-                for (int jb = 0; jb < 2; jb++) {
+            for (int ib = 0; ib < BR; ib++)
+                for (int jb = 0; jb < BC; jb++) {
                     dCB[ib][jb] = w;
                     w += (R0[ib + 1] - R0[ib]) * (C0[jb + 1] - C0[jb]) * clen;
                 }
         }
         // evaluations: A rows I, B columns J, C blocks (I, J), each in its own point-tiled layout
-        uint32_t *EA[2], *EB[2], *EC[2][2];
-        PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan) + 16 * 256));
+        uint32_t *EA[BR], *EB[BC], *EC[BR][BC];
+        PMLG_TRY(ws_reserve(ctx, &ctx->ws, product_scratch_bytes(j, plan) + (BR + BC + BR * BC) * 256));
         {
             char *w = (char *)ctx->ws.ptr;
             auto take = [&](int64_t nent) {
@@ -474,10 +488,10 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
                 w += align256((size_t)(N * nent) * 4);
                 return r_;
             };
-            for (int ib = 0; ib < 2; ib++) EA[ib] = take((R0[ib + 1] - R0[ib]) * k);
-            for (int jb = 0; jb < 2; jb++) EB[jb] = take(k * (C0[jb + 1] - C0[jb]));
-            for (int ib = 0; ib < 2; ib++)
-                for (int jb = 0; jb < 2; jb++) EC[ib][jb] = take((R0[ib + 1] - R0[ib]) * (C0[jb + 1] - C0[jb]));
+            for (int ib = 0; ib < BR; ib++) EA[ib] = take((R0[ib + 1] - R0[ib]) * k);
+            for (int jb = 0; jb < BC; jb++) EB[jb] = take(k * (C0[jb + 1] - C0[jb]));
+            for (int ib = 0; ib < BR; ib++)
+                for (int jb = 0; jb < BC; jb++) EC[ib][jb] = take((R0[ib + 1] - R0[ib]) * (C0[jb + 1] - C0[jb]));
         }
         // the product of block (I, J) and its buffers
         auto block_job = [&](int ib, int jb, ProductJob &bj, ProductBufs &bb) {
@@ -496,19 +510,20 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
         PMLG_TRY(next_event(st, &e));
         PMLG_CUDA_TRY(cudaStreamWaitEvent(hs, e, 0));
         PMLG_CUDA_TRY(cudaStreamWaitEvent(ds, e, 0));
-        cudaEvent_t bev[2], aev[2];
-        for (int q = 0; q < 4; q++) {   // B columns 0, A rows 0, B columns 1, A rows 1
-            const int h = q >> 1;
-            if ((q & 1) == 0) {
-                const int64_t bw = C0[h + 1] - C0[h];
-                PMLG_CUDA_TRY(cudaMemcpy2DAsync(dBJ[h], (size_t)(bw * len2) * 8, B + C0[h] * len2,
+        cudaEvent_t bev[BC], aev[BR];
+        const int nsteps = BR > BC ? BR : BC;
+        for (int q = 0; q < nsteps; q++) {   // B columns q, A rows q
+            if (q < BC) {
+                const int64_t bw = C0[q + 1] - C0[q];
+                PMLG_CUDA_TRY(cudaMemcpy2DAsync(dBJ[q], (size_t)(bw * len2) * 8, B + C0[q] * len2,
                                                 (size_t)(c * len2) * 8, (size_t)(bw * len2) * 8, (size_t)k,
                                                 cudaMemcpyHostToDevice, hs));
-                PMLG_TRY(next_event(hs, &bev[h]));
-            } else {
-                PMLG_TRY(h2d(ctx, dA + R0[h] * k * len1, A + R0[h] * k * len1,
-                             (size_t)((R0[h + 1] - R0[h]) * k * len1) * 8, hs));
-                PMLG_TRY(next_event(hs, &aev[h]));
+                PMLG_TRY(next_event(hs, &bev[q]));
+            }
+            if (q < BR) {
+                PMLG_TRY(h2d(ctx, dA + R0[q] * k * len1, A + R0[q] * k * len1,
+                             (size_t)((R0[q + 1] - R0[q]) * k * len1) * 8, hs));
+                PMLG_TRY(next_event(hs, &aev[q]));
             }
         }
         auto run_block = [&](int ib, int jb) -> int {
@@ -525,24 +540,24 @@ PMLG_API int pmlg_poly_mat_mul_host(pmlg_ctx *ctx, uint64_t *C, const uint64_t *
                                             cudaMemcpyDeviceToHost, ds));
             return PMLG_OK;
         };
-        auto fwd_half = [&](int which, int h) -> int {   // A rows h (which 0) or B columns h (which 1)
+        auto fwd_block = [&](int which, int h) -> int {   // A rows h (which 0) or B columns h (which 1)
             ProductJob bj;
             ProductBufs bb;
             block_job(which == 0 ? h : 0, which == 0 ? 0 : h, bj, bb);
             return product_forward(ctx, bj, plan, bb, which, 0, which == 0 ? bj.r * k : k * bj.c, st);
         };
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, bev[0], 0));
-        PMLG_TRY(fwd_half(1, 0));
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, aev[0], 0));
-        PMLG_TRY(fwd_half(0, 0));
-        PMLG_TRY(run_block(0, 0));
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, bev[1], 0));
-        PMLG_TRY(fwd_half(1, 1));
-        PMLG_TRY(run_block(0, 1));
-        PMLG_CUDA_TRY(cudaStreamWaitEvent(st, aev[1], 0));
-        PMLG_TRY(fwd_half(0, 1));
-        PMLG_TRY(run_block(1, 0));
-        PMLG_TRY(run_block(1, 1));
+        for (int q = 0; q < nsteps; q++) {
+            if (q < BC) {
+                PMLG_CUDA_TRY(cudaStreamWaitEvent(st, bev[q], 0));
+                PMLG_TRY(fwd_block(1, q));
+                for (int ib = 0; ib < q && ib < BR; ib++) PMLG_TRY(run_block(ib, q));
+            }
+            if (q < BR) {
+                PMLG_CUDA_TRY(cudaStreamWaitEvent(st, aev[q], 0));
+                PMLG_TRY(fwd_block(0, q));
+                for (int jb = 0; jb <= q && jb < BC; jb++) PMLG_TRY(run_block(q, jb));
+            }
+        }
         PMLG_TRY(next_event(ds, &e));
         PMLG_CUDA_TRY(cudaStreamWaitEvent(st, e, 0));
         return device_status(ctx, st);

@@ -260,13 +260,16 @@ def test_batched_uneven(ctx):
         assert np.array_equal(to_host(o), ref)
 
 
-@pytest.mark.parametrize("dims", [(7, 5, 3, 60, 45), (1, 4, 4, 33, 20), (3, 3, 9, 128, 100), (16, 16, 16, 256, 256)])
+@pytest.mark.parametrize("dims", [(7, 5, 3, 60, 45), (1, 4, 4, 33, 20), (3, 3, 9, 128, 100), (16, 16, 16, 256, 256),
+                                  (5, 6, 8, 70, 50), (2, 3, 2, 40, 40)])
 @pytest.mark.parametrize("prime", ["ntt", "p59", "p30"])
 def test_host_path_row_blocks(ctx, dims, prime):
-    """The host-buffer product copies B first and A in row blocks whose rows of C go
-    back while the next rows of A arrive: row counts that do not divide into the
-    blocks, one row, and moduli that take one NTT prime or CRT over several,
-    bit-exact against the oracle and against the device entry point."""
+    """The host-buffer product overlaps the copies in both directions: with one NTT
+    prime it computes blocks of rows x columns of C (each goes back while the rest of
+    A and B arrive), with CRT it copies B first and A in row blocks.  Row and column
+    counts that do not divide into the blocks, one row, fewer columns than column
+    blocks, and moduli that take one NTT prime or CRT over several, bit-exact against
+    the oracle and against the device entry point."""
     import pml_gb300
     r, k, c, l1, l2 = dims
     p = {"ntt": P998, "p59": oracle.rand_prime(59, 77), "p30": oracle.rand_prime(30, 78)}[prime]
