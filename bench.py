@@ -42,6 +42,7 @@ P = 998244353
 R = K = C = 64
 LEN = 4096
 PM_M, PM_N, PM_ORDER = 64, 32, 8192
+P60 = 576460752303423619   # the reference's 60-bit test prime (testing_collection.h:16-20)
 WORKLOAD = "nmod_poly_mat_mul 64x64 . 64x64, len 4096 (deg < 4096), p = 998244353, uniform coefficients"
 METRIC = "exact poly_mat_mul & pmbasis time: INT8 split-limb TC vs CUDA-core form, 1 GB300"
 
@@ -56,13 +57,14 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the pointwise-batch and batched-uneven measurements")
-    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven", "kernel", "layout", "dot"],
+    ap.add_argument("--profile-case", choices=["product", "pmbasis", "pwbatch", "uneven", "kernel", "layout", "dot",
+                                               "pmbasis_word"],
                     default=None,
                     help="run one product per form (or one pmbasis at order 1024, one 4096-product "
                          "pointwise batch per form, one batched-uneven call with the FP16 form, one kernel "
                          "basis of a 64x32 degree-255 matrix, one layout conversion each way at 64x64 x 4096, "
-                         "one call of each dot-product kernel on about 256 MB) "
-                         "and exit: the small cases for kernel captures")
+                         "one call of each dot-product kernel on about 256 MB, one pmbasis 64x32 at order 64 "
+                         "modulo a 60-bit prime) and exit: the small cases for kernel captures")
     return ap.parse_args()
 
 
@@ -113,6 +115,13 @@ def run_profile_case(args):
         Q = pml_gb300.nmod_poly_mat_set_trunc_from_mat_poly(M, 4096, ctx=ctx)
         torch.cuda.synchronize()
         print(json.dumps({"profile_case": "layout", "exact": bool(torch.equal(Pm, Q)), "launches": ctx.launches}))
+    elif args.profile_case == "pmbasis_word":
+        import oracle
+        F = oracle.rand_poly_mat(PM_M, PM_N, 64, P60, 5)
+        ab, sh = pml_gb300.nmod_poly_mat_pmbasis(torch.from_numpy(F.view(np.int64)).cuda(), 64, [0] * PM_M, P60,
+                                                 ctx=ctx)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_case": "pmbasis_word", "rdeg_sum": int(sum(sh)), "launches": ctx.launches}))
     else:
         rng = np.random.default_rng(7)
         F = rng.integers(0, P, size=(PM_M, PM_N, 1024), dtype=np.uint64)
@@ -292,6 +301,10 @@ def cpu_baselines():
         "ms_1_thread_order1024": _timed(lambda: oracle.pmbasis(F[:, :, :1024], 1024, [0] * PM_M, P, nthreads=1)),
         "sample": "all cores: the full order-8192 call; 1 thread: the same input truncated to order 1024 "
                   "(the 1-thread full call would take minutes)"}
+    Fw = oracle.rand_poly_mat(PM_M, PM_N, 256, P60, 61)
+    res["pmbasis_64x32_order256_p60"] = {
+        "ms_all_cores": _timed(lambda: oracle.pmbasis(Fw, 256, [0] * PM_M, P60, nthreads=nt)),
+        "sample": "pmbasis 64x32 at order 256 modulo the 60-bit prime, all cores, one call"}
     inst = uneven_instances(5)
     sub = inst[:64]
     macs = lambda L: sum(A.shape[0] ** 3 * A.shape[2] for A, _, _ in L)
@@ -613,6 +626,29 @@ def measure_dixon(ctx, dev, st, rank):
             "timing": "wall clock around one call after one warm-up call"}
 
 
+def measure_pmbasis_word(ctx, dev, st, rank):
+    """pmbasis of a 64x32 matrix modulo the reference's 60-bit test prime (the 64-bit leaf and
+    the products by CRT over NTT primes), zero shift, at orders 256 and 1024; wall clock
+    around one call (it synchronises) after one warm-up call."""
+    import time
+    import torch
+    import pml_gb300
+    out = {}
+    for order in (256, 1024):
+        rng = np.random.default_rng(61 + rank)
+        F = torch.from_numpy((rng.integers(0, P60, size=(PM_M, PM_N, order), dtype=np.uint64)).view(np.int64)).to(dev)
+        pml_gb300.nmod_poly_mat_pmbasis(F, order, [0] * PM_M, P60, ctx=ctx)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ab, sh = pml_gb300.nmod_poly_mat_pmbasis(F, order, [0] * PM_M, P60, ctx=ctx)
+        torch.cuda.synchronize()
+        out[f"order{order}_ms"] = (time.perf_counter() - t0) * 1e3
+        out[f"order{order}_rdeg_sum"] = int(sum(sh))
+    out["config"] = f"pmbasis 64x32, zero shift, p = {P60} (60 bits), uniform coefficients"
+    out["timing"] = "wall clock around one call after one warm-up call"
+    return out
+
+
 def measure_popov(ctx, dev, st, rank):
     """Shift-Popov approximant basis of a 64x32 matrix at order 1024, zero shift
     (popov_pmbasis: two pmbasis calls and the leading-matrix normalisation); wall clock
@@ -875,6 +911,7 @@ def run_pml(args):
         "dot_products": measure_dot_products(ctx, dev, st, rank, peaks.get("hbm_gbs")),
         "dixon": measure_dixon(ctx, dev, st, rank),
         "popov_pmbasis": measure_popov(ctx, dev, st, rank),
+        "pmbasis_word_prime": measure_pmbasis_word(ctx, dev, st, rank),
     }
 
     # CPU baseline (rank 0, N = 1): oracle port, 1 thread (the reference is single-threaded)

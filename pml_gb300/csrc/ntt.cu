@@ -561,63 +561,77 @@ ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
 // the mixed-radix digits stay in registers; every residue of a coefficient is loaded
 // before any arithmetic.  The primes are in (2^29.8, 2^30): a Shoup product is below
 // 2 q_j and the running value below 2 q_j + 2^30 < 2^32, so the inner Horner steps
-// need no reduction, and two conditional subtractions bring it below q_j.
-template <int T>
+// need no reduction, and two conditional subtractions bring it below q_j.  WIDE: p is
+// above every prime, so the digits need no reduction mod p.
+template <int T, bool WIDE>
 __global__ void __launch_bounds__(256)
 crt_kernel(CrtPlan plan, const uint32_t *__restrict__ res32, int64_t nent, int64_t cnt,
            uint64_t *__restrict__ out64, int64_t out_ld, int64_t out_cap)
 {
+    const int64_t plane = nent * cnt;
     // entries along grid y, coefficients along x (no 64-bit division per element)
-    for (int64_t e = blockIdx.y; e < nent; e += gridDim.y)
-    for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < out_cap;
-         d += (int64_t)gridDim.x * blockDim.x) {
-        if (d >= cnt) {
-            out64[e * out_ld + d] = 0;
-            continue;
-        }
-        uint32_t c[T];
-#pragma unroll
-        for (int j = 0; j < T; j++) c[j] = __ldg(res32 + (j * nent + e) * cnt + d);
-#pragma unroll
-        for (int j = 1; j < T; j++) {
-            const uint32_t qj = plan.q[j];
-            // c_0 + c_1 q_0 + ... + c_{j-1} q_0..q_{j-2} modulo q_j
-            uint32_t v = c[j - 1];
-#pragma unroll
-            for (int l = j - 2; l >= 0; l--) v = shoup_mul(v, plan.qmod[j][l], plan.qmodq[j][l], qj) + c[l];
-            v = min(v, v - 2 * qj);
-            v = min(v, v - qj);
-            const uint32_t r = c[j];
-            const uint32_t diff = r + qj - v;   // in [1, 2 q_j)
-            const uint32_t cj = shoup_mul(diff, plan.ginv[j], plan.ginvq[j], qj);
-            c[j] = min(cj, cj - qj);
-        }
-        const uint64_t p = plan.p;
-        uint64_t res;
-        if (p <= (1ull << 63)) {
-            // Horner x <- x q_l + c_l mod p with 64-bit Shoup products (results in [0, 2p))
-            auto red = [&](uint64_t v) {   // v < 2^32 -> [0, p)
-                uint64_t r = v - __umul64hi(v, plan.onepq) * p;
-                return r >= p ? r - p : r;
-            };
-            uint64_t x = red(c[T - 1]);
-#pragma unroll
-            for (int l = T - 2; l >= 0; l--) {
-                x = x * plan.qp[l] - __umul64hi(x, plan.qpq[l]) * p;
-                x = x >= p ? x - p : x;
-                const uint64_t cl = red(c[l]);
-                const uint64_t s = x + cl;
-                x = (s < x || s >= p) ? s - p : s;
+    for (int64_t e = blockIdx.y; e < nent; e += gridDim.y) {
+        const uint32_t *rp = res32 + e * cnt;
+        uint64_t *op = out64 + e * out_ld;
+        for (int64_t d = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; d < out_cap;
+             d += (int64_t)gridDim.x * blockDim.x) {
+            if (d >= cnt) {
+                op[d] = 0;
+                continue;
             }
-            res = x;
-        } else {
-            unsigned __int128 x = c[T - 1] % p;
+            uint32_t c[T];
 #pragma unroll
-            for (int l = T - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
-            res = (uint64_t)x;
+            for (int j = 0; j < T; j++) c[j] = __ldg(rp + j * plane + d);
+#pragma unroll
+            for (int j = 1; j < T; j++) {
+                const uint32_t qj = plan.q[j];
+                // c_0 + c_1 q_0 + ... + c_{j-1} q_0..q_{j-2} modulo q_j
+                uint32_t v = c[j - 1];
+#pragma unroll
+                for (int l = j - 2; l >= 0; l--) v = shoup_mul(v, plan.qmod[j][l], plan.qmodq[j][l], qj) + c[l];
+                v = min(v, v - 2 * qj);
+                v = min(v, v - qj);
+                const uint32_t diff = c[j] + qj - v;   // in [1, 2 q_j)
+                const uint32_t cj = shoup_mul(diff, plan.ginv[j], plan.ginvq[j], qj);
+                c[j] = min(cj, cj - qj);
+            }
+            const uint64_t p = plan.p;
+            uint64_t res;
+            if (p <= (1ull << 63)) {
+                // Horner x <- x q_l + c_l mod p with 64-bit Shoup products (results in [0, 2p))
+                auto red = [&](uint64_t v) {   // v < 2^32 -> [0, p)
+                    if (WIDE) return v;
+                    uint64_t r = v - __umul64hi(v, plan.onepq) * p;
+                    return r >= p ? r - p : r;
+                };
+                uint64_t x = red(c[T - 1]);
+#pragma unroll
+                for (int l = T - 2; l >= 0; l--) {
+                    x = x * plan.qp[l] - __umul64hi(x, plan.qpq[l]) * p;
+                    x = x >= p ? x - p : x;
+                    const uint64_t s = x + red(c[l]);
+                    x = (s < x || s >= p) ? s - p : s;
+                }
+                res = x;
+            } else {
+                unsigned __int128 x = c[T - 1] % p;
+#pragma unroll
+                for (int l = T - 2; l >= 0; l--) x = (x * plan.q[l] + c[l]) % p;
+                res = (uint64_t)x;
+            }
+            op[d] = res;
         }
-        out64[e * out_ld + d] = res;
     }
+}
+
+template <int T>
+static void crt_launch(const CrtPlan &plan, dim3 grid, const uint32_t *res32, int64_t nent, int64_t cnt,
+                       uint64_t *out64, int64_t out_ld, int64_t out_cap, cudaStream_t st)
+{
+    if (plan.p > (1ull << 30))
+        crt_kernel<T, true><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap);
+    else
+        crt_kernel<T, false><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap);
 }
 
 // ---------------------------------------------------------------------------
@@ -800,12 +814,12 @@ int crt_combine(pmlg_ctx *ctx, const CrtPlan &plan, const uint32_t *res32, int64
     const dim3 grid((unsigned)bx, (unsigned)by);
     prof_begin(ctx, "crt", st);
     switch (plan.t) {
-    case 1: crt_kernel<1><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
-    case 2: crt_kernel<2><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
-    case 3: crt_kernel<3><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
-    case 4: crt_kernel<4><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
-    case 5: crt_kernel<5><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
-    default: crt_kernel<6><<<grid, 256, 0, st>>>(plan, res32, nent, cnt, out64, out_ld, out_cap); break;
+    case 1: crt_launch<1>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
+    case 2: crt_launch<2>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
+    case 3: crt_launch<3>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
+    case 4: crt_launch<4>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
+    case 5: crt_launch<5>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
+    default: crt_launch<6>(plan, grid, res32, nent, cnt, out64, out_ld, out_cap, st); break;
     }
     prof_end(ctx, st);
     count_launch(ctx);
