@@ -177,12 +177,32 @@ __device__ __forceinline__ constexpr int grp_poff(int s)
     return G == 4 ? (s << LLS) + ((s << LLS) >> 4) : s;
 }
 
-template <int G, int LLS, int SPAN>
+// ROT (layouts of 16 consecutive residues per thread, G < 4): register chunk c
+// (v[4c .. 4c+3]) holds the residues of slot chunk (c + r) & 3, r = (t >> 1) & 3.  A
+// group of at most 2 levels works on aligned runs of 2^G <= 4 slots, so it computes
+// the same on rotated registers.  The persistent inverse reads its point tiles (64
+// contiguous bytes per thread) in this order: its 16-byte shared-memory loads are then
+// conflict-free (in natural order, four lanes of every eight share a bank).  Measured
+// on the forward kernel's staging stores as well, the rotation cost more than the
+// conflicts it removed (0.122 against 0.115 ms), so only the inverse uses it.
+__device__ __forceinline__ int rot_chunk(int t, int c) { return (c + ((t >> 1) & 3)) & 3; }
+
+template <int G, int LLS, int SPAN, bool ROT = false>
 __device__ __forceinline__ void regs_to_smem_t(uint32_t *x, const uint32_t (&v)[16], int t)
 {
     uint32_t *p = x + grp_pbase<G, LLS, SPAN>(t);
+    if constexpr (ROT) {
+        static_assert(G < 4, "rotation of 16 consecutive residues");
 #pragma unroll
-    for (int s = 0; s < 16; s++) p[grp_poff<G, LLS>(s)] = v[s];
+        for (int c = 0; c < 4; c++) {
+            uint32_t *pc = p + 4 * rot_chunk(t, c);
+#pragma unroll
+            for (int u = 0; u < 4; u++) pc[u] = v[4 * c + u];
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < 16; s++) p[grp_poff<G, LLS>(s)] = v[s];
+    }
 }
 
 template <int G, int LLS, int SPAN>
@@ -228,9 +248,19 @@ __device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t
     }
 }
 
+// whether the first inverse group is at most radix-4, so that its registers may be
+// rotated by whole chunks of four
+template <int LG>
+__device__ __forceinline__ constexpr bool rot_ok()
+{
+    return LG >= 12 && InvGeom<LG, 0>::G <= 2;
+}
+
 // The first group writes its layout without a barrier: a caller that reuses x for
 // another transform separates the last reads of the previous one from it.
-template <int LG, int GI>
+// ROT: the registers arrive rotated (see rot_chunk); the first group writes them back
+// to their places
+template <int LG, int GI, bool ROT = false>
 __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t, const NttDev &T)
 {
     if constexpr (GI < InvGeom<LG, 0>::NG) {
@@ -245,8 +275,8 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
         }
         if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
         dit_const<Gm::G>(v, T);
-        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
-        inv_groups<LG, GI + 1>(v, x, t, T);
+        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN, ROT && GI == 0>(x, v, t);
+        inv_groups<LG, GI + 1, false>(v, x, t, T);
     }
 }
 
@@ -542,14 +572,15 @@ ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
         }
         if (!done && a.err) atomicExch(a.err, 1);
         uint32_t v[16];
+        constexpr bool ROT = rot_ok<LG>();
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-            const uint4 o = *reinterpret_cast<const uint4 *>(pf + 16 * t + 4 * c);
+            const uint4 o = *reinterpret_cast<const uint4 *>(pf + 16 * t + 4 * (ROT ? rot_chunk(t, c) : c));
             v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
         }
         __syncthreads();   // the buffer is read: the next transform may come in
         if (t == 0 && done && e + gridDim.x < a.nent) prefetch(e + gridDim.x);
-        inv_groups<LG, 0>(v, x, t, T);
+        inv_groups<LG, 0, ROT>(v, x, t, T);
         inv_store<LG>(v, a, e, j, t, T.q);
         if (!__syncthreads_and(done)) break;   // a load that never completed ends the CTA's work
     }
