@@ -9,7 +9,7 @@
 // applied once per residue, after the group for decimation in frequency and
 // before it for decimation in time: slot m gets w_span^(off * bitrev4(m)).
 // Between groups the residues go through shared memory (padded by one word
-// every 16 against bank conflicts).  Forward transforms are decimation in
+// every 16, or 32, against bank conflicts).  Forward transforms are decimation in
 // frequency (natural order in, bit-reversed out), inverse ones decimation in
 // time (bit-reversed in, natural out): no reordering pass.  Values stay in
 // [0, 2q) between forward butterflies and in [0, 4q) between inverse ones
@@ -22,7 +22,6 @@
 
 namespace pmlg {
 
-__device__ __forceinline__ int sidx(int i) { return i + (i >> 4); }
 
 // Cache policy: coefficients and evaluations stream through once and are not
 // kept in L1 (no_allocate); the group twiddle tables are kept (evict_last).
@@ -133,9 +132,14 @@ __device__ __forceinline__ void group_twiddles(uint32_t (&v)[16], const NttDev &
 // ---------------------------------------------------------------------------
 // Kernels, one instantiation per transform size 2^LG: every group's shape is a
 // compile-time constant, so the shared-memory exchange is one base address per
-// thread plus immediate offsets.  With the padding sidx(i) = i + i/16, the
-// padded index of slot s is sidx(base(t)) + sidx(c_s), because c_s is either
-// a multiple of 16 or cannot carry the base across a multiple of 16.
+// thread plus immediate offsets.  With the padding sidx(i) = i + (i >> PS) (one
+// word every 2^PS), the padded index of slot s is sidx(base(t)) + sidx(c_s),
+// because c_s is either a multiple of 2^PS or cannot carry the base across one.
+// PS = 4 everywhere but in the forward kernels from N = 2^13 on, where one word
+// every 32 leaves fewer bank conflicts in the exchanges (2-way ones in the radix-2
+// spaced layout instead of the 512- and 32-spaced ones: 512 instead of 768 extra
+// wavefronts per transform) and measured 0.1108 against 0.1144 ms per forward
+// launch at the headline product; the inverse kernels measured no gain from it.
 // ---------------------------------------------------------------------------
 
 template <int LG, int GI>
@@ -159,22 +163,22 @@ struct InvGeom
 };
 
 // padded shared-memory index of slot 0 of thread t in a group (G, LLS, SPAN)
-template <int G, int LLS, int SPAN>
+template <int G, int LLS, int SPAN, int PS>
 __device__ __forceinline__ int grp_pbase(int t)
 {
     if constexpr (G == 4) {
         const int base = (t >> LLS) * SPAN + (t & ((1 << LLS) - 1));
-        return base + (base >> 4);
+        return base + (base >> PS);
     } else {
-        return 17 * t;   // 16 consecutive residues per thread
+        return 16 * t + ((16 * t) >> PS);   // 16 consecutive residues per thread
     }
 }
 
 // padded offset of slot s relative to grp_pbase
-template <int G, int LLS>
+template <int G, int LLS, int PS>
 __device__ __forceinline__ constexpr int grp_poff(int s)
 {
-    return G == 4 ? (s << LLS) + ((s << LLS) >> 4) : s;
+    return G == 4 ? (s << LLS) + ((s << LLS) >> PS) : s;
 }
 
 // ROT (layouts of 16 consecutive residues per thread, G < 4): register chunk c
@@ -187,10 +191,10 @@ __device__ __forceinline__ constexpr int grp_poff(int s)
 // conflicts it removed (0.122 against 0.115 ms), so only the inverse uses it.
 __device__ __forceinline__ int rot_chunk(int t, int c) { return (c + ((t >> 1) & 3)) & 3; }
 
-template <int G, int LLS, int SPAN, bool ROT = false>
+template <int G, int LLS, int SPAN, int PS, bool ROT = false>
 __device__ __forceinline__ void regs_to_smem_t(uint32_t *x, const uint32_t (&v)[16], int t)
 {
-    uint32_t *p = x + grp_pbase<G, LLS, SPAN>(t);
+    uint32_t *p = x + grp_pbase<G, LLS, SPAN, PS>(t);
     if constexpr (ROT) {
         static_assert(G < 4, "rotation of 16 consecutive residues");
 #pragma unroll
@@ -201,16 +205,16 @@ __device__ __forceinline__ void regs_to_smem_t(uint32_t *x, const uint32_t (&v)[
         }
     } else {
 #pragma unroll
-        for (int s = 0; s < 16; s++) p[grp_poff<G, LLS>(s)] = v[s];
+        for (int s = 0; s < 16; s++) p[grp_poff<G, LLS, PS>(s)] = v[s];
     }
 }
 
-template <int G, int LLS, int SPAN>
+template <int G, int LLS, int SPAN, int PS>
 __device__ __forceinline__ void smem_to_regs_t(uint32_t (&v)[16], const uint32_t *x, int t)
 {
-    const uint32_t *p = x + grp_pbase<G, LLS, SPAN>(t);
+    const uint32_t *p = x + grp_pbase<G, LLS, SPAN, PS>(t);
 #pragma unroll
-    for (int s = 0; s < 16; s++) v[s] = p[grp_poff<G, LLS>(s)];
+    for (int s = 0; s < 16; s++) v[s] = p[grp_poff<G, LLS, PS>(s)];
 }
 
 // Barriers between groups.  A group reads its layout from shared memory and writes
@@ -233,17 +237,18 @@ __device__ __forceinline__ void fwd_groups(uint32_t (&v)[16], uint32_t *x, int t
     if constexpr (GI < FwdGeom<LG, 0>::NG) {
         using Gm = FwdGeom<LG, GI>;
         constexpr bool TW = Gm::G == 4 && Gm::LLS > 0;
+        constexpr int PS = LG >= 13 ? 5 : 4;
         if constexpr (GI > 0) {
             using Gp = FwdGeom<LG, GI - 1>;
             if constexpr (warp_local_layout<LG, Gp::G, Gp::LLS>() && warp_local_layout<LG, Gm::G, Gm::LLS>())
                 __syncwarp();
             else
                 __syncthreads();
-            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
+            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN, PS>(v, x, t);
         }
         dif_const<Gm::G, ZH && GI == 0, TW>(v, T);
         if constexpr (TW) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
-        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN>(x, v, t);
+        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN, PS>(x, v, t);
         fwd_groups<LG, GI + 1, ZH>(v, x, t, T);
     }
 }
@@ -271,11 +276,11 @@ __device__ __forceinline__ void inv_groups(uint32_t (&v)[16], uint32_t *x, int t
                 __syncwarp();
             else
                 __syncthreads();
-            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN>(v, x, t);
+            smem_to_regs_t<Gm::G, Gm::LLS, Gm::SPAN, 4>(v, x, t);
         }
         if constexpr (Gm::G == 4 && Gm::LLS > 0) group_twiddles(v, T, t & ((1 << Gm::LLS) - 1), Gm::LLS);
         dit_const<Gm::G>(v, T);
-        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN, ROT && GI == 0>(x, v, t);
+        if constexpr (GI < Gm::NG - 1) regs_to_smem_t<Gm::G, Gm::LLS, Gm::SPAN, 4, ROT && GI == 0>(x, v, t);
         inv_groups<LG, GI + 1, false>(v, x, t, T);
     }
 }
@@ -308,8 +313,10 @@ struct NttBlock
     // resident CTAs the kernels ask registers for (per-thread register budgets above)
     static constexpr int FWD_MIN = min_ctas(PMLG_NTT_FWD_REGS);
     static constexpr int INV_MIN = min_ctas(PMLG_NTT_INV_REGS);
-    // persistent inverse: shared memory (transform + prefetch) allows 6 / 3 / 1 CTAs
-    static constexpr int INVP_MIN = LG <= 12 ? 6 : LG == 13 ? 3 : 1;
+    // persistent inverse: shared memory (transform + prefetch) allows 6 / 3 / 1 CTAs;
+    // at N = 2^13 two CTAs per SM with 64 registers (no spills) measured 0.136 ms per
+    // launch at the headline product against 0.147 for three with 40 (44 bytes spilled)
+    static constexpr int INVP_MIN = LG <= 12 ? 6 : LG == 13 ? 2 : 1;
 };
 
 // Loads the first group (elements t + m N/16) and runs all groups; with ZH the
@@ -519,10 +526,11 @@ ntt_inv_persist_kernel(NttInvArgs a)
 // The same, with the point tiles brought in by TMA tensor loads (256 tiles per
 // box, one transform = N / 1024 boxes) completing on an mbarrier; the wait is
 // bounded (on time-out the error word is set and the results are invalid).
-// Used up to N = 2^13 (32 KB per transform and mbarrier phase).  At N = 2^14,
-// where one phase expects 64 KB, this kernel returned wrong transforms for
-// about 0.5% of the entries of a 2048-entry launch on GB300, while the cp.async
-// kernel above was exact on the same inputs, so that size uses the cp.async one.
+// Used up to N = 2^13 (32 KB per transform and mbarrier phase).  At N = 2^14 this
+// kernel once returned wrong transforms for about 0.5% of the entries of a
+// 2048-entry launch, before the proxy fence below was added (the fence later
+// removed the same kind of errors at 2^12 and 2^13); that size has not been
+// measured again and keeps the cp.async kernel above.
 template <int LG>
 __global__ void __launch_bounds__(NttBlock<LG>::THREADS, NttBlock<LG>::INVP_MIN)
 ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
@@ -578,6 +586,11 @@ ntt_inv_tma_kernel(NttInvArgs a, const __grid_constant__ CUtensorMap tmap)
             const uint4 o = *reinterpret_cast<const uint4 *>(pf + 16 * t + 4 * (ROT ? rot_chunk(t, c) : c));
             v[4 * c + 0] = o.x; v[4 * c + 1] = o.y; v[4 * c + 2] = o.z; v[4 * c + 3] = o.w;
         }
+        // The next TMA load writes this buffer through the async proxy: without a proxy
+        // fence after the generic reads, the barrier alone does not order them before it
+        // (without the fence, 2 CTAs per SM at N = 2^13 returned a wrong entry in about
+        // 1% of the headline products, 4 CTAs per SM at N = 2^12 in 70%).
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();   // the buffer is read: the next transform may come in
         if (t == 0 && done && e + gridDim.x < a.nent) prefetch(e + gridDim.x);
         inv_groups<LG, 0, ROT>(v, x, t, T);
@@ -793,6 +806,8 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a0, cudaStream_t st)
         // persistent: as many CTAs as fit on the GPU, each walking over transforms
         const int N = 1 << a.lg;
         const size_t smp = (size_t)(2 * N + (N >> 4)) * sizeof(uint32_t);
+        // CTAs launched per SM; at N = 2^13 two are resident, and the third wave still
+        // measured faster (0.137 against 0.142 ms per headline launch)
         const int per_sm = a.lg == 12 ? 6 : a.lg == 13 ? 3 : 1;
         int64_t g = (int64_t)ctx->sm_count * per_sm;
         if (g > a.nent) g = a.nent;
