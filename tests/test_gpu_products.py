@@ -137,6 +137,27 @@ def test_products_full_width_16384(fctx, dims):
     assert np.array_equal(_mul(fctx, A, B, P998), oracle.poly_mat_mul_ntt(A, B, P998, nthreads=16))
 
 
+@pytest.mark.parametrize("length", [2048, 4096])
+def test_products_repeated(ctx, length):
+    """The same 64x64 product (transforms of 4096 and 8192 points, the persistent
+    inverse with its TMA prefetch) repeated 300 times, every result compared with the
+    oracle's: an ordering error between the prefetch and the reads of its buffer shows
+    up as a wrong entry in a small fraction of the calls, not in every call."""
+    import pml_gb300
+    torch = _torch()
+    A = oracle.rand_poly_mat(64, 64, length, P998, 71)
+    B = oracle.rand_poly_mat(64, 64, length, P998, 72)
+    ref = torch.from_numpy(oracle.poly_mat_mul_ntt(A, B, P998, nthreads=16).view(np.int64)).cuda()
+    dA, dB = to_dev(A), to_dev(B)
+    ctx.set_form(3)
+    bad = 0
+    for _ in range(300):
+        C = pml_gb300.nmod_poly_mat_multiply(dA, dB, P998, ctx=ctx)
+        bad += int((C != ref).any().item())
+    ctx.set_form(0)
+    assert bad == 0
+
+
 def test_products_config1_plain(fctx):
     """16x16 . 16x16, degree < 256, p = 998244353 (the CPU-runnable case)."""
     p = P998
