@@ -364,7 +364,7 @@ def run_reference(args):
 # still in L2 when the kernel ends
 TRAFFIC_SOURCE = ("constant from one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of "
                   "`python bench.py --profile-case product`, not measured in this run")
-NCU_TRAFFIC = {"ntt_fwd": 217.1e6, "ntt_inv": 360.3e6, "pointwise_f16_tc": 368.2e6,
+NCU_TRAFFIC = {"ntt_fwd": 216.6e6, "ntt_inv": 347.2e6, "pointwise_f16_tc": 368.2e6,
                "pointwise_int8_tc": 370.8e6, "pointwise_cuda_core": 367.1e6}
 
 
