@@ -613,13 +613,18 @@ pw_f16_kernel(PwArgs a)
         // result.  With SKIP (every shape below 64 x 64) a warp without any skips the
         // region but still waits for it and reports it drained, so every mbarrier phase
         // keeps its arrival count; the write-out reads only outputs that are in the result.
+        // Unpacked with SKIP, the two warps of a lane quarter swap their 16-column halves
+        // from one point to the next: with 3 of the 4 column granules in the result (33 to
+        // 48 columns) each then computes 3 granules per two points instead of 4 and 2.
         const bool packed = lmt < 6;
-        const bool use0 = !SKIP || (packed ? (sp & 1) == 0 : 32 * (sp & 1) < a.r && 16 * ch < a.c);
-        const bool use1 = !SKIP || (packed ? (sp & 1) == 1 : 32 * (sp & 1) < a.r && 32 + 16 * ch < a.c);
+        const bool alt = SKIP && !packed;
         uint32_t p = 0;
         for (int64_t gc = blockIdx.x; gc < nunits; gc += gridDim.x) {
             for (int pp = 0; pp < 2; pp++, p++) {
                 uint32_t *row = Cst + (pp * 2 + hi) * F16_CST_WORDS + i * F16_CST_LD;
+                const int chp = alt ? ch ^ (int)(p & 1u) : ch;
+                const bool use0 = !SKIP || (packed ? (sp & 1) == 0 : 32 * (sp & 1) < a.r && 16 * chp < a.c);
+                const bool use1 = !SKIP || (packed ? (sp & 1) == 1 : 32 * (sp & 1) < a.r && 32 + 16 * chp < a.c);
                 for (int h = 0; h < 2; h++) {
                     const bool useful = h ? use1 : use0;
                     uint64_t acc[16];
@@ -632,7 +637,7 @@ pw_f16_kernel(PwArgs a)
                             uint32_t v[3][16];
 #pragma unroll
                             for (int j = 0; j < 3; j++)
-                                TC_LD16(lane_base + (uint32_t)(256 * h + 96 * s + 32 * j + 16 * ch), v[j]);
+                                TC_LD16(lane_base + (uint32_t)(256 * h + 96 * s + 32 * j + 16 * chp), v[j]);
                             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
                             for (int j = 0; j < 3; j++)
@@ -650,7 +655,7 @@ pw_f16_kernel(PwArgs a)
                         for (int u = 0; u < 16; u++) r[u] = mod64_q_2(acc[u] + koff, q, a.r32, a.r32q, a.oneq);
 #pragma unroll
                         for (int m = 0; m < 4; m++)
-                            *reinterpret_cast<uint4 *>(row + 32 * h + 16 * ch + 4 * m) =
+                            *reinterpret_cast<uint4 *>(row + 32 * h + 16 * chp + 4 * m) =
                                 make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
                     }
                 }
