@@ -806,10 +806,10 @@ int ntt_inverse(pmlg_ctx *ctx, const NttInvArgs &a0, cudaStream_t st)
         // persistent: as many CTAs as fit on the GPU, each walking over transforms
         const int N = 1 << a.lg;
         const size_t smp = (size_t)(2 * N + (N >> 4)) * sizeof(uint32_t);
-        // CTAs launched per SM; at N = 2^13 two are resident, and more waves still balance
-        // the work better (per headline launch: 0.142 ms with 2 per SM, 0.137 with 3,
-        // 0.1345 with 4, 0.1342 with 6)
-        const int per_sm = a.lg == 12 ? 6 : a.lg == 13 ? 4 : 1;
+        // CTAs launched per SM; at N = 2^13 two are resident, at 2^12 six, and more waves
+        // still balance the work better (per 4096-transform launch at 2^13: 0.142 ms with
+        // 2 per SM, 0.137 with 3, 0.1345 with 4; at 2^12: 0.0655 with 6, 0.0634 with 12)
+        const int per_sm = a.lg == 12 ? 12 : a.lg == 13 ? 4 : 1;
         int64_t g = (int64_t)ctx->sm_count * per_sm;
         if (g > a.nent) g = a.nent;
         const dim3 grid((unsigned)g, a.t);
