@@ -539,7 +539,20 @@ __global__ void l64s_update(Leaf64Args a, int ord)
         uint64_t *dst = base + (d + K - off[row]) * pl + (int64_t)row * width + col;
         const uint64_t *src = base + (d + K) * pl + col;
         uint64_t acc = *dst;
-        for (int b = 0; b < rank; b++)
+        // eight pivot rows at a time: their loads are issued together instead of one
+        // global-memory latency per pivot row
+        int b = 0;
+        for (; b + 8 <= rank; b += 8) {
+            uint64_t xv[8], pv[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                xv[u] = xr[b + u];
+                pv[u] = src[(int64_t)prow[b + u] * width - poff[b + u] * pl];
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) acc = M.add(acc, M.mul(xv[u], pv[u]));
+        }
+        for (; b < rank; b++)
             acc = M.add(acc, M.mul(xr[b], src[(int64_t)prow[b] * width - poff[b] * pl]));
         *dst = acc;
     }
