@@ -415,6 +415,10 @@ l64s_elim(Leaf64Args a, int ord)
     // pivot value.
     unsigned usedbits = 0;   // bit k of lane l: row 32 k + l holds a pivot
     int rk = 0, nn = 0;
+    // up to 64 columns and 32 rows: one thread per column and two rows of E
+    const bool small = m <= 64 && n <= 32 && nth == 1024;
+    const int mycol = tid & 63, myrow = tid >> 6;
+    bool mynp = false;   // this thread's column is a non-pivot column
     for (int c = 0; c < m; c++) {
         int pl = -1;
         for (int k = 0, base = 0; base < n && pl < 0; k++, base += 32) {
@@ -425,6 +429,7 @@ l64s_elim(Leaf64Args a, int ord)
         }
         if (pl < 0) {
             if (tid == 0) nonpiv[nn] = c;
+            if (mycol == c) mynp = true;
             nn++;
             __syncthreads();
             continue;
@@ -436,7 +441,18 @@ l64s_elim(Leaf64Args a, int ord)
         rk++;
         const int W = nn + (m - 1 - c);   // columns updated
         const int tot = (n - 1) * W;
-        if (tot > 0) {
+        if (small) {
+            // thread = (column, rows r and r + 16): the same entries as below, without
+            // the index arithmetic
+            if (mycol < m && mycol != c && (mycol > c || mynp)) {
+                const uint64_t er = E[pl * ldE + mycol];
+                for (int j = myrow; j < n; j += 16) {
+                    if (j == pl) continue;
+                    uint64_t *e = E + j * ldE + mycol;
+                    *e = l64_fms(M, pv, *e, E[j * ldE + c], er);
+                }
+            }
+        } else if (tot > 0) {
             int jj = tid / W, w = tid - jj * W;
             const int dj = nth / W, dw = nth - dj * W;
             const uint64_t *er = E + pl * ldE;
